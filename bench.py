@@ -1,0 +1,340 @@
+"""Benchmark: systems solved per second at relative residual 1e-10.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--quick]
+
+Headline workload: ParILU(0) (5 sweeps) + ISAI(L, U on |T|^2) preconditioned
+BiCGSTAB of 4096 FP64 systems on a 3D 7-point 10x10x10 pattern (n = 1000,
+nnz = 6400), seeded synthetic values, relative tolerance 1e-10.  One step =
+one solve of the whole batch (preconditioner generation + iteration) through
+the library's C ABI.  `value` is measured with the inputs resident in HBM;
+`e2e` adds the pinned host->device copy of the step's values and right-hand
+sides and the device->host copy of the solutions and per-system results.
+
+Under torchrun (N > 1) every rank solves its own full batch on its own GPU
+(weak scaling, no collective on the data path); the step time is the maximum
+over ranks.  --impl reference times the CPU restatement of the reference's
+solver (the reference has no CPU path of its own) on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _sub in ("merging-ilu0_gb300", "oracle", "tests"):
+    sys.path.insert(0, os.path.join(ROOT, _sub))
+
+SEED = 20261203
+METRIC = "systems solved/sec at rel. residual 1e-10: chosen vs plain form, % HBM roofline"
+
+# workloads: (kind, gx, gy, gz, nsys, options)
+HEADLINE = dict(name="parilu5_isai_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096,
+                desc="ParILU(0) 5 sweeps + ISAI(L,U on |T|^2) BiCGSTAB, 4096 FP64 systems, 3D 7-point 10x10x10 "
+                     "(n=1000, nnz=6400), Peclet skew U(0,0.5), rel. tol 1e-10, max 500 iterations",
+                opts=dict(precond=4, parilu_sweeps=5, isai_power=2, tol_mode=1, tol=1e-10, max_iter=500,
+                          reduction=1, factor_precision=0))
+SECONDARY = [
+    dict(name="plain_ilu0_2d5_16x16_fast", kind=1, grid=(16, 16, 1), nsys=16384,
+         desc="plain form: merged ILU(0) BiCGSTAB, 16384 FP64 systems, 2D 5-point 16x16, rel 1e-10, FAST order",
+         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1)),
+    dict(name="plain_ilu0_2d5_16x16_ref", kind=1, grid=(16, 16, 1), nsys=16384,
+         desc="plain form in the reference's operation order (bit-identical iterates)",
+         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=0)),
+    dict(name="fp32_ilu0_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768,
+         desc="FP32-stored ILU(0) factors (FP64 recurrences), 32768 convection-diffusion systems 24x24",
+         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1)),
+    dict(name="fp64_ilu0_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768,
+         desc="same workload with FP64 factors",
+         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=0)),
+]
+
+
+def bytes_per_system(n, nnz):
+    """Compulsory HBM bytes of one solved system: A values, b, x, 24 B of results."""
+    return 8 * nnz + 16 * n + 24
+
+
+def fp64_flops_per_iter(n, nnz, prec_nnz, precond):
+    """FP64 operations of one full BiCGSTAB iteration (2 per FMA): two SpMVs with A, two
+    preconditioner applications (ISAI: two SpMVs; LU: two triangular solves), six inner products
+    and the vector updates."""
+    fma = 2 * nnz + 6 * n + 6 * n
+    fma += 2 * prec_nnz
+    return 2 * fma
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 2 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip() == "Active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_port_rate(wl, sample, threads=None):
+    """Systems/s of the oracle (CPU restatement of the reference path) on a bounded sample."""
+    import bilu
+    import helpers as H
+    import oracle as O
+    if threads:
+        O.set_num_threads(threads)
+    kind, (gx, gy, gz) = wl["kind"], wl["grid"]
+    rp, ci, v, b = bilu.gen_stencil(kind, gx, gy, gz, sample, SEED)
+    o = wl["opts"]
+    t0 = time.perf_counter()
+    r = H.oracle_pipeline(rp, ci, v, b, o["precond"], approach=o.get("ilu_approach", 1),
+                          sweeps=o.get("parilu_sweeps", 5), fp32=o.get("factor_precision", 0) == 1,
+                          tol_mode=o.get("tol_mode", 0), tol=o.get("tol", 1e-11), max_iter=o.get("max_iter", 500))
+    dt = time.perf_counter() - t0
+    return sample / dt, dt, O.num_threads(), float(r["iters"].mean())
+
+
+def run_reference_arm(args):
+    """--impl reference: the CPU restatement of the reference's solver on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle as O
+    wl = HEADLINE
+    sample = 48
+    for _ in range(args.warmup):
+        cpu_port_rate(wl, 8)
+    rates, secs = [], []
+    for _ in range(args.steps):
+        rate, dt, cores, _ = cpu_port_rate(wl, sample)
+        rates.append(rate)
+        secs.append(dt)
+    value = statistics.median(rates)
+    line = {"metric": METRIC, "value": value, "unit": "systems/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * statistics.median(secs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["desc"], "nsys_per_step": sample},
+            "cpu_baseline": {"value": value, "unit": "systems/s", "cores": O.num_threads(), "kind": "port",
+                             "sample": f"{sample} systems of the headline workload per step, full pipeline "
+                                       f"(ParILU sweeps, ISAI, BiCGSTAB) in the reference's operation order"},
+            "e2e": {"value": value, "unit": "systems/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def measure(wl, steps, warmup, dev, stream, sampler=None, e2e=False, timed_hook=None):
+    import torch
+    import bilu
+    kind, (gx, gy, gz), nsys = wl["kind"], wl["grid"], wl["nsys"]
+    rp, ci, v, b = bilu.gen_stencil(kind, gx, gy, gz, nsys, SEED)
+    n, nnz = len(rp) - 1, len(ci)
+    plan = bilu.Plan(rp, ci, **wl["opts"])
+    plan.enable_timing(True)
+    V = torch.from_numpy(v).to(dev)
+    B = torch.from_numpy(b).to(dev)
+    X = torch.empty_like(B)
+    it = torch.empty(nsys, dtype=torch.float32, device=dev)
+    cv = torch.empty(nsys, dtype=torch.int32, device=dev)
+    rs = torch.empty(nsys, dtype=torch.float64, device=dev)
+    tr = torch.empty(nsys, dtype=torch.float64, device=dev)
+    st = torch.empty(nsys, dtype=torch.int32, device=dev)
+    del v, b
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            plan.solve(V, B, X, it, cv, rs, tr, st, stream=stream)
+        torch.cuda.synchronize()
+        setup, solve = [], []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if timed_hook:
+            timed_hook("begin")
+        if sampler:
+            sampler.start()
+        e0.record(stream)
+        for _ in range(steps):
+            plan.solve(V, B, X, it, cv, rs, tr, st, stream=stream)
+            t = plan.last_timing()
+            setup.append(t["setup_ms"])
+            solve.append(t["solve_ms"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        clocks = sampler.stop() if sampler else None
+        if timed_hook:
+            timed_hook("end")
+        ms = e0.elapsed_time(e1)
+    iters = it.cpu().numpy()
+    conv = cv.cpu().numpy()
+    trn = tr.cpu().numpy()
+    bn = B.norm(dim=1).cpu().numpy()
+    info = plan.info()
+    out = {"name": wl["name"], "nsys": nsys, "n": n, "nnz": nnz, "ms_total": ms, "steps": steps,
+           "systems_per_s": nsys * steps / (ms / 1e3), "setup_ms": statistics.mean(setup),
+           "solve_ms": statistics.mean(solve), "mean_iters": float(iters.mean()), "max_iters": float(iters.max()),
+           "converged": int((conv == 1).sum()), "max_rel_true_res": float((trn / bn).max()), "info": info,
+           "clocks": clocks}
+    if e2e:
+        # end to end through the C ABI with host buffers: H2D of values and b, solve, D2H of x and results
+        hv = torch.empty(V.shape, dtype=V.dtype, pin_memory=True)
+        hv.copy_(V)
+        hb = torch.empty(B.shape, dtype=B.dtype, pin_memory=True)
+        hb.copy_(B)
+        hx = torch.empty(B.shape, dtype=B.dtype, pin_memory=True)
+        hit = torch.empty(nsys, dtype=torch.float32, pin_memory=True)
+        hcv = torch.empty(nsys, dtype=torch.int32, pin_memory=True)
+        hrs = torch.empty(nsys, dtype=torch.float64, pin_memory=True)
+        with torch.cuda.stream(stream):
+            torch.cuda.synchronize()
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for _ in range(steps):
+                V.copy_(hv, non_blocking=True)
+                B.copy_(hb, non_blocking=True)
+                plan.solve(V, B, X, it, cv, rs, tr, st, stream=stream)
+                hx.copy_(X, non_blocking=True)
+                hit.copy_(it, non_blocking=True)
+                hcv.copy_(cv, non_blocking=True)
+                hrs.copy_(rs, non_blocking=True)
+            f1.record(stream)
+            torch.cuda.synchronize()
+            ems = f0.elapsed_time(f1)
+        out["e2e"] = {"value": nsys * steps / (ems / 1e3), "unit": "systems/s",
+                      "h2d_bytes_per_step": int(hv.numel() * 8 + hb.numel() * 8),
+                      "d2h_bytes_per_step": int(hx.numel() * 8 + nsys * (4 + 4 + 8))}
+        if not (conv == 1).all():
+            out["e2e"]["note"] = "not every system converged"
+    plan.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="headline only, no secondary workloads")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    import torch
+    import bilu
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream(dev)
+
+    def barrier(_what):
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    res = measure(HEADLINE, args.steps, max(args.warmup, 3), dev, stream, sampler=sampler, e2e=True,
+                  timed_hook=barrier)
+    ms = res["ms_total"]
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        e = torch.tensor([res["e2e"]["value"]], device=dev)
+        dist.all_reduce(e, op=dist.ReduceOp.SUM)
+        res["e2e"]["value"] = float(e.item())
+    value = HEADLINE["nsys"] * args.steps * world / (ms / 1e3)
+    secondary = []
+    if rank == 0 and not args.quick:
+        for wl in SECONDARY:
+            try:
+                r = measure(wl, 2, 1, dev, stream)
+                secondary.append({k: r[k] for k in ("name", "nsys", "systems_per_s", "setup_ms", "solve_ms",
+                                                    "mean_iters", "converged", "max_rel_true_res")} |
+                                 {"workload": wl["desc"]})
+            except Exception as ex:  # a secondary workload never hides the headline
+                secondary.append({"name": wl["name"], "error": str(ex)})
+    if rank != 0:
+        return
+    n, nnz, nsys = res["n"], res["nnz"], res["nsys"]
+    info = res["info"]
+    hbm, peak_kind = load_peaks()
+    bps = bytes_per_system(n, nnz)
+    solve_s = res["solve_ms"] / 1e3
+    achieved = bps * nsys / solve_s / 1e9
+    prec_nnz = info["nnz_isai_L"] + info["nnz_isai_U"]
+    flops = fp64_flops_per_iter(n, nnz, prec_nnz, HEADLINE["opts"]["precond"]) * res["mean_iters"] * nsys
+    fp64_peak = 1205.0  # GFLOP/s: 602.5 G DFMA/s measured on this machine's GB300 (full-warp DFMA stream)
+    cores = os.cpu_count()
+    rate, dt, used, _ = cpu_port_rate(HEADLINE, 32)
+    line = {
+        "metric": METRIC, "value": value, "unit": "systems/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": HEADLINE["desc"], "nsys": nsys, "n": n, "nnz": nnz, "reduction": "fast",
+                   "factor_precision": "fp64", "threads_per_system": info["threads"],
+                   "smem_bytes_per_system": info["smem_bytes"],
+                   "l2": "inputs larger than L2: A values %.0f MB per step" % (nsys * nnz * 8 / 1e6),
+                   "parallelism": f"weak: {world} independent batch(es), one per GPU"},
+        "clocks": res["clocks"],
+        "e2e": res["e2e"],
+        "gpu_launches": 3 * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_bicgstab (solver)",
+                     "bytes_per_system": bps},
+        "roofline_fp64": {"achieved": flops / solve_s / 1e9, "peak": fp64_peak, "unit": "GFLOP/s",
+                          "frac": flops / solve_s / 1e9 / fp64_peak,
+                          "note": "FP64 issue, not HBM, bounds this kernel on GB300"},
+        "stages_ms": {"setup": res["setup_ms"], "solve": res["solve_ms"]},
+        "solve_quality": {"mean_iters": res["mean_iters"], "max_iters": res["max_iters"],
+                          "converged": res["converged"], "max_rel_true_residual": res["max_rel_true_res"]},
+        "cpu_baseline": {"value": rate, "unit": "systems/s", "cores": used, "kind": "port",
+                         "sample": f"32 systems of the headline workload through the CPU restatement "
+                                   f"({dt:.2f} s, {used} OpenMP threads of {cores} host cores)"},
+        "secondary": secondary,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

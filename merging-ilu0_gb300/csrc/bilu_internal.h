@@ -1,0 +1,120 @@
+// Internal declarations shared by the host plan code (bilu_plan.cpp) and the
+// CUDA kernels (k_*.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "bilu.h"
+
+namespace bilu {
+
+// Records the message for bilu_last_error() and returns the code.
+bilu_status set_error(bilu_status code, const std::string& msg);
+
+// Device views of one pattern plan (all pointers into one device allocation).
+struct DevPattern {
+  int n = 0, nnz = 0;
+  // operator pattern = the caller's pattern (SpMV with A, true residual)
+  int a_nnz = 0;
+  const int* a_rp = nullptr;
+  const int* a_ci = nullptr;
+  int a_maxl = 0;               // longest row of the operator pattern
+  const int* rp = nullptr;      // n+1   factor pattern (A with diagonals)
+  const int* ci = nullptr;      // nnz
+  const int* diag = nullptr;    // n     position of (i,i)
+  const int* row_of = nullptr;  // nnz   row of each entry
+  // level schedules of the unit-lower and upper triangular solves
+  int nlev_lo = 0, nlev_up = 0, maxw_lo = 0, maxw_up = 0;
+  const int* lev_lo_ptr = nullptr;   // nlev_lo+1
+  const int* lev_lo_rows = nullptr;  // n (rows in level order)
+  const int* lev_up_ptr = nullptr;
+  const int* lev_up_rows = nullptr;
+  // factorisation dependencies per entry: pairs (pos l_ik, pos u_kj) with k
+  // ascending, k < min(i, j)
+  const int* dep_ptr = nullptr;  // nnz+1
+  const int2* dep = nullptr;     // ndep
+  // ISAI patterns and per-row solve programs
+  int ail_nnz = 0, aiu_nnz = 0;
+  const int* ail_rp = nullptr;
+  const int* ail_ci = nullptr;
+  const int* aiu_rp = nullptr;
+  const int* aiu_ci = nullptr;
+  // program per ISAI row: blocks {t, k} followed by k entries {c, pos}
+  const int* ail_prog_ptr = nullptr;  // n+1 (in int2 units)
+  const int2* ail_prog = nullptr;
+  const int* aiu_prog_ptr = nullptr;
+  const int2* aiu_prog = nullptr;
+  // input -> factor pattern value map (src index or -1 for inserted diagonals)
+  int nnz_in = 0;
+  const int* src_map = nullptr;  // nnz
+  // reference L / U split maps: factor position of each L / U entry (-1 = unit diagonal)
+  int nnz_L = 0, nnz_U = 0;
+  const int* l_src = nullptr;
+  const int* u_src = nullptr;
+};
+
+// Shared-memory carve-up of the solver kernel for one system (byte offsets;
+// -1 = operand read from global memory instead).
+struct SmemLayout {
+  int A = -1;      // double[nnz]
+  int F = -1;      // factors: FT[nnz]
+  int ail = -1;    // FT[ail_nnz]
+  int aiu = -1;    // FT[aiu_nnz]
+  int rinv = -1;   // double[n] (FP64) / float[n] (FP32)
+  int vec = -1;    // 7 double vectors of n (x, r/s, r_hat, p, v, t, p_hat/s_hat)
+  int fvec = -1;   // 2 float vectors of n (FP32 preconditioner scratch)
+  int tmpv = -1;   // 1 double vector of n (ISAI intermediate / ILU scratch)
+  int red = -1;    // 64 doubles of scalars
+  int total = 0;
+};
+
+enum PrecKind : int {
+  PK_ILU_INKERNEL = 0,  // factorise inside the solver kernel (merged)
+  PK_LU_GLOBAL = 1,     // in-place factors given in global memory
+  PK_ISAI = 2,          // aiL / aiU given in global memory
+  PK_NONE = 3,
+};
+
+struct SolveArgs {
+  DevPattern pat;
+  SmemLayout lay;
+  int nsys = 0;
+  const double* A = nullptr;   // nsys*a_nnz, operator (caller's) pattern
+  const double* b = nullptr;
+  double* x = nullptr;
+  const void* F = nullptr;     // PK_LU_GLOBAL factors (double or float)
+  const void* ail = nullptr;   // PK_ISAI
+  const void* aiu = nullptr;
+  float* iters = nullptr;
+  int* conv = nullptr;
+  double* res = nullptr;
+  int* status = nullptr;
+  double* true_res = nullptr;  // fused true-residual epilogue when non-null
+  double tol = 1e-11;
+  int tol_mode = BILU_TOL_ABS;
+  int max_iter = 500;
+  int prec = PK_ILU_INKERNEL;
+  int approach = 1;
+  int dot_serial = 0;  // 1: serial inner products (ISAI solver family, reference order)
+};
+
+// kernel launch wrappers (k_solve.cu / k_factor.cu)
+cudaError_t launch_solve(const SolveArgs& a, int threads, int fp32, int reduce_fast, int maxl, cudaStream_t st);
+size_t solve_max_smem();
+cudaError_t launch_expand(const DevPattern& p, int nsys, const double* vin, double* vout, cudaStream_t st);
+cudaError_t launch_ilu0(const DevPattern& p, int nsys, const double* A, double* lu, int approach, int threads,
+                        cudaStream_t st);
+cudaError_t launch_parilu0(const DevPattern& p, int nsys, const double* A, const double* init, double* lu,
+                           int sweeps, int threads, cudaStream_t st);
+cudaError_t launch_isai(const DevPattern& p, int nsys, const double* lu, void* ail, void* aiu, int fp32,
+                        int threads, cudaStream_t st);
+cudaError_t launch_to_float(const double* a, float* b, size_t n, cudaStream_t st);
+cudaError_t launch_split(const DevPattern& p, int nsys, const double* lu, double* L, double* U, cudaStream_t st);
+cudaError_t launch_true_residual(const DevPattern& p, int nsys, const double* A, const double* b, const double* x,
+                                 double* out, int threads, cudaStream_t st);
+
+}  // namespace bilu

@@ -1,0 +1,794 @@
+// Host side of the C ABI: pattern analysis (missing diagonals, diagonal
+// pointers, L/U split, level schedules, factorisation dependency lists, ISAI
+// patterns and per-row solve programs), the shared-memory layout of the
+// solver kernel, and the entry points declared in include/bilu.h.
+//
+// Reference host code this replaces (paths inside Batched-ILU0-merged/ILU0_ISAI_bicgstab/):
+//   factorization.cu:399-575   missing diagonals, diagonal pointers, L/U row pointers and fill
+//   parILU_0_gpu.cu:118-220    create_dependency_graph_parilu (built once per plan here,
+//                              not once per call after six device-to-host copies)
+//   ILU_0_gpu.cu:693-756, 947-1053  dependency lists of approaches 3 and 4
+//   isai_gpu.cu:40-179         pattern of |A|^power (sparse here, not a dense n^3 product)
+//   *_gpu.cu helpers           Batched_*_Gpu_helper launch sequences
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bilu.h"
+#include "bilu_internal.h"
+
+namespace bilu {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+bilu_status set_error(bilu_status code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+}  // namespace bilu
+
+using namespace bilu;
+
+struct bilu_plan {
+  bilu_options opts;
+  int device = 0;
+  int n = 0, nnz_in = 0, nnz = 0, missing = 0;
+  std::vector<int> in_rp, in_ci;      // caller's pattern
+  std::vector<int> rp, ci, diag, row_of, src;
+  std::vector<int> lev_lo_ptr, lev_lo_rows, lev_up_ptr, lev_up_rows;
+  int maxw_lo = 0, maxw_up = 0, maxl = 0, a_maxl = 0;
+  std::vector<int> dep_ptr;
+  std::vector<int> dep;  // pairs
+  std::vector<int> l_rp, l_ci, l_src, u_rp, u_ci, u_src;
+  bool has_isai = false;
+  std::vector<int> ail_rp, ail_ci, aiu_rp, aiu_ci;
+  std::vector<int> ail_prog_ptr, ail_prog, aiu_prog_ptr, aiu_prog;  // prog in int units (pairs)
+  int* dbuf = nullptr;
+  DevPattern dp;
+  // solver kernel configuration
+  int threads = 0;
+  SmemLayout lay;
+  // workspace
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  // stage timing events (PST / IST / OET)
+  bool timing = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+};
+
+namespace plan_detail {
+
+bool is_fp32(const bilu_options& o) { return o.factor_precision == BILU_FP32; }
+bool is_isai(int p) { return p == BILU_PRECOND_ILU0_ISAI || p == BILU_PRECOND_PARILU0_ISAI; }
+
+int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+bilu_status cuda_err(cudaError_t e, const char* what) {
+  return set_error(BILU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// position of column c in row r of (rp, ci), or -1
+int find_pos(const std::vector<int>& rp, const std::vector<int>& ci, int r, int c) {
+  auto b = ci.begin() + rp[r], e = ci.begin() + rp[r + 1];
+  auto it = std::lower_bound(b, e, c);
+  if (it != e && *it == c) return (int)(it - ci.begin());
+  return -1;
+}
+
+// levels: lower solve (row depends on its strictly-lower columns) and upper
+// solve (row depends on its strictly-upper columns)
+void build_levels(bilu_plan& P) {
+  const int n = P.n;
+  std::vector<int> lev(n, 0);
+  int nl = 0;
+  for (int i = 0; i < n; ++i) {
+    int l = 0;
+    for (int k = P.rp[i]; k < P.diag[i]; ++k) l = std::max(l, lev[P.ci[k]] + 1);
+    lev[i] = l;
+    nl = std::max(nl, l + 1);
+  }
+  auto bucket = [&](const std::vector<int>& lv, int nlev, std::vector<int>& ptr, std::vector<int>& rows, int& maxw) {
+    ptr.assign(nlev + 1, 0);
+    for (int i = 0; i < n; ++i) ptr[lv[i] + 1]++;
+    for (int l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
+    rows.assign(n, 0);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (int i = 0; i < n; ++i) rows[fill[lv[i]]++] = i;
+    maxw = 0;
+    for (int l = 0; l < nlev; ++l) maxw = std::max(maxw, ptr[l + 1] - ptr[l]);
+  };
+  bucket(lev, nl, P.lev_lo_ptr, P.lev_lo_rows, P.maxw_lo);
+  std::vector<int> levu(n, 0);
+  int nu = 0;
+  for (int i = n - 1; i >= 0; --i) {
+    int l = 0;
+    for (int k = P.diag[i] + 1; k < P.rp[i + 1]; ++k) l = std::max(l, levu[P.ci[k]] + 1);
+    levu[i] = l;
+    nu = std::max(nu, l + 1);
+  }
+  bucket(levu, nu, P.lev_up_ptr, P.lev_up_rows, P.maxw_up);
+}
+
+// (l_ik, u_kj) pairs per entry, k ascending, k < min(i, j)
+void build_deps(bilu_plan& P) {
+  P.dep_ptr.assign(P.nnz + 1, 0);
+  P.dep.clear();
+  for (int i = 0; i < P.n; ++i)
+    for (int e = P.rp[i]; e < P.rp[i + 1]; ++e) {
+      const int j = P.ci[e];
+      const int kmax = std::min(i, j);
+      for (int lk = P.rp[i]; lk < P.rp[i + 1] && P.ci[lk] < kmax; ++lk) {
+        const int k = P.ci[lk];
+        const int uk = find_pos(P.rp, P.ci, k, j);
+        if (uk >= 0) {
+          P.dep.push_back(lk);
+          P.dep.push_back(uk);
+        }
+      }
+      P.dep_ptr[e + 1] = (int)(P.dep.size() / 2);
+    }
+}
+
+// structural pattern of T^power, T given by (trp, tci)
+void pattern_power(int n, const std::vector<int>& trp, const std::vector<int>& tci, int power, std::vector<int>& orp,
+                   std::vector<int>& oci) {
+  std::vector<int> crp = trp, cci = tci;
+  std::vector<char> mark(n, 0);
+  std::vector<int> row;
+  for (int p = 2; p <= power; ++p) {
+    std::vector<int> nrp(n + 1, 0), nci;
+    // (T * C)(r, :) = union over k in T(r, :) of C(k, :)
+    for (int r = 0; r < n; ++r) {
+      row.clear();
+      for (int a = trp[r]; a < trp[r + 1]; ++a) {
+        const int k = tci[a];
+        for (int b = crp[k]; b < crp[k + 1]; ++b) {
+          const int c = cci[b];
+          if (!mark[c]) {
+            mark[c] = 1;
+            row.push_back(c);
+          }
+        }
+      }
+      std::sort(row.begin(), row.end());
+      for (int c : row) mark[c] = 0;
+      nci.insert(nci.end(), row.begin(), row.end());
+      nrp[r + 1] = (int)nci.size();
+    }
+    crp.swap(nrp);
+    cci.swap(nci);
+  }
+  orp.swap(crp);
+  oci.swap(cci);
+}
+
+bilu_status build_isai(bilu_plan& P) {
+  const int n = P.n;
+  const int power = std::max(1, P.opts.isai_power);
+  pattern_power(n, P.l_rp, P.l_ci, power, P.ail_rp, P.ail_ci);
+  pattern_power(n, P.u_rp, P.u_ci, power, P.aiu_rp, P.aiu_ci);
+  // lower programs
+  P.ail_prog_ptr.assign(n + 1, 0);
+  P.ail_prog.clear();
+  for (int i = 0; i < n; ++i) {
+    const int beg = P.ail_rp[i], sz = P.ail_rp[i + 1] - beg;
+    if (sz > 32)
+      return set_error(BILU_ERR_CAPACITY, "ISAI row " + std::to_string(i) + " of aiL has " + std::to_string(sz) +
+                                              " entries (limit 32, isai_gpu.cu:223)");
+    if (sz < 1 || P.ail_ci[beg + sz - 1] != i) return set_error(BILU_ERR_PATTERN, "ISAI(L) row without its diagonal");
+    for (int t = sz - 2; t >= 0; --t) {
+      const size_t hdr = P.ail_prog.size();
+      P.ail_prog.push_back(t);
+      P.ail_prog.push_back(0);
+      int cnt = 0;
+      for (int c = sz - 1; c > t; --c) {
+        const int pos = find_pos(P.rp, P.ci, P.ail_ci[beg + c], P.ail_ci[beg + t]);
+        if (pos >= 0) {
+          P.ail_prog.push_back(c);
+          P.ail_prog.push_back(pos);
+          ++cnt;
+        }
+      }
+      P.ail_prog[hdr + 1] = cnt;
+    }
+    P.ail_prog_ptr[i + 1] = (int)(P.ail_prog.size() / 2);
+  }
+  P.aiu_prog_ptr.assign(n + 1, 0);
+  P.aiu_prog.clear();
+  for (int i = 0; i < n; ++i) {
+    const int beg = P.aiu_rp[i], sz = P.aiu_rp[i + 1] - beg;
+    if (sz > 32)
+      return set_error(BILU_ERR_CAPACITY, "ISAI row " + std::to_string(i) + " of aiU has " + std::to_string(sz) +
+                                              " entries (limit 32, isai_gpu.cu:223)");
+    if (sz < 1 || P.aiu_ci[beg] != i) return set_error(BILU_ERR_PATTERN, "ISAI(U) row without its diagonal");
+    for (int t = 1; t < sz; ++t) {
+      const size_t hdr = P.aiu_prog.size();
+      P.aiu_prog.push_back(t);
+      P.aiu_prog.push_back(0);
+      int cnt = 0;
+      for (int c = 0; c < t; ++c) {
+        const int pos = find_pos(P.rp, P.ci, P.aiu_ci[beg + c], P.aiu_ci[beg + t]);
+        if (pos >= 0) {
+          P.aiu_prog.push_back(c);
+          P.aiu_prog.push_back(pos);
+          ++cnt;
+        }
+      }
+      P.aiu_prog[hdr + 1] = cnt;
+    }
+    P.aiu_prog_ptr[i + 1] = (int)(P.aiu_prog.size() / 2);
+  }
+  return BILU_OK;
+}
+
+// Shared-memory layout of the solver kernel and its CTA size.
+void choose_layout(bilu_plan& P) {
+  const bilu_options& o = P.opts;
+  const int n = P.n;
+  const bool fp32 = is_fp32(o);
+  const bool fast = o.reduction == BILU_REDUCE_FAST;
+  const int fts = fp32 ? 4 : 8;
+  const int prec = o.precond;
+  const bool lu_prec = !(is_isai(prec) || prec == BILU_PRECOND_NONE);
+  int off = 0;
+  auto take = [&](int bytes) {
+    const int o2 = off;
+    off = round_up(off + bytes, 16);
+    return o2;
+  };
+  SmemLayout L;
+  L.red = take(128);
+  int vec_doubles = 7 * n;
+  if (prec == BILU_PRECOND_ILU0 && fp32) vec_doubles = std::max(vec_doubles, P.nnz);  // FP64 factorisation scratch
+  L.vec = take(vec_doubles * 8);
+  if (fp32) L.fvec = take(2 * n * 4);
+  if (is_isai(prec) && !fp32) L.tmpv = take(n * 8);
+  if (lu_prec && (fp32 || fast)) L.rinv = take(n * fts);
+  const int budget = (int)solve_max_smem();
+  // staging, most-reused operand first
+  if (lu_prec) {
+    if (prec == BILU_PRECOND_ILU0 || off + P.nnz * fts <= budget) L.F = take(P.nnz * fts);
+  } else if (is_isai(prec)) {
+    if (off + P.ail_rp[n] * fts <= budget) L.ail = take(P.ail_rp[n] * fts);
+    if (off + P.aiu_rp[n] * fts <= budget) L.aiu = take(P.aiu_rp[n] * fts);
+  }
+  if (off + P.nnz_in * 8 <= budget) L.A = take(P.nnz_in * 8);
+  L.total = off;
+  P.lay = L;
+  int th = o.threads_per_system > 0 ? o.threads_per_system : round_up(std::max(n, 64), 32);
+  th = std::min(round_up(std::max(th, 32), 32), 1024);
+  P.threads = th;
+}
+
+bilu_status upload(bilu_plan& P) {
+  std::vector<int> buf;
+  auto put = [&](const std::vector<int>& v) {
+    while (buf.size() % 4) buf.push_back(0);  // 16-byte alignment
+    const size_t o = buf.size();
+    buf.insert(buf.end(), v.begin(), v.end());
+    if (v.empty()) buf.push_back(0);
+    return o;
+  };
+  const size_t o_in_rp = put(P.in_rp), o_in_ci = put(P.in_ci);
+  const size_t o_rp = put(P.rp), o_ci = put(P.ci), o_diag = put(P.diag), o_row = put(P.row_of), o_src = put(P.src);
+  const size_t o_llp = put(P.lev_lo_ptr), o_llr = put(P.lev_lo_rows), o_lup = put(P.lev_up_ptr),
+               o_lur = put(P.lev_up_rows);
+  const size_t o_dp = put(P.dep_ptr), o_dep = put(P.dep);
+  const size_t o_lsrc = put(P.l_src), o_usrc = put(P.u_src);
+  size_t o_alrp = 0, o_alci = 0, o_aurp = 0, o_auci = 0, o_alpp = 0, o_alp = 0, o_aupp = 0, o_aup = 0;
+  if (P.has_isai) {
+    o_alrp = put(P.ail_rp);
+    o_alci = put(P.ail_ci);
+    o_aurp = put(P.aiu_rp);
+    o_auci = put(P.aiu_ci);
+    o_alpp = put(P.ail_prog_ptr);
+    o_alp = put(P.ail_prog);
+    o_aupp = put(P.aiu_prog_ptr);
+    o_aup = put(P.aiu_prog);
+  }
+  cudaError_t e = cudaMalloc((void**)&P.dbuf, buf.size() * sizeof(int));
+  if (e != cudaSuccess) return set_error(BILU_ERR_ALLOC, std::string("plan upload: ") + cudaGetErrorString(e));
+  e = cudaMemcpy(P.dbuf, buf.data(), buf.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_err(e, "plan upload");
+  DevPattern& d = P.dp;
+  const int* b = P.dbuf;
+  d.n = P.n;
+  d.nnz = P.nnz;
+  d.a_nnz = P.nnz_in;
+  d.a_rp = b + o_in_rp;
+  d.a_ci = b + o_in_ci;
+  d.a_maxl = P.a_maxl;
+  d.rp = b + o_rp;
+  d.ci = b + o_ci;
+  d.diag = b + o_diag;
+  d.row_of = b + o_row;
+  d.nlev_lo = (int)P.lev_lo_ptr.size() - 1;
+  d.nlev_up = (int)P.lev_up_ptr.size() - 1;
+  d.maxw_lo = P.maxw_lo;
+  d.maxw_up = P.maxw_up;
+  d.lev_lo_ptr = b + o_llp;
+  d.lev_lo_rows = b + o_llr;
+  d.lev_up_ptr = b + o_lup;
+  d.lev_up_rows = b + o_lur;
+  d.dep_ptr = b + o_dp;
+  d.dep = reinterpret_cast<const int2*>(b + o_dep);
+  d.nnz_in = P.nnz_in;
+  d.src_map = b + o_src;
+  d.nnz_L = (int)P.l_src.size();
+  d.nnz_U = (int)P.u_src.size();
+  d.l_src = b + o_lsrc;
+  d.u_src = b + o_usrc;
+  if (P.has_isai) {
+    d.ail_nnz = P.ail_rp[P.n];
+    d.aiu_nnz = P.aiu_rp[P.n];
+    d.ail_rp = b + o_alrp;
+    d.ail_ci = b + o_alci;
+    d.aiu_rp = b + o_aurp;
+    d.aiu_ci = b + o_auci;
+    d.ail_prog_ptr = b + o_alpp;
+    d.ail_prog = reinterpret_cast<const int2*>(b + o_alp);
+    d.aiu_prog_ptr = b + o_aupp;
+    d.aiu_prog = reinterpret_cast<const int2*>(b + o_aup);
+  }
+  return BILU_OK;
+}
+
+bilu_status ensure_ws(bilu_plan* P, size_t bytes) {
+  if (bytes <= P->ws_bytes) return BILU_OK;
+  if (P->ws) cudaFree(P->ws);
+  P->ws = nullptr;
+  P->ws_bytes = 0;
+  cudaError_t e = cudaMalloc(&P->ws, bytes);
+  if (e != cudaSuccess) return set_error(BILU_ERR_ALLOC, std::string("workspace: ") + cudaGetErrorString(e));
+  P->ws_bytes = bytes;
+  return BILU_OK;
+}
+
+size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+bilu_status check_opts(const bilu_options* o) {
+  if (!o) return BILU_OK;
+  if (o->precond < 0 || o->precond > BILU_PRECOND_NONE) return set_error(BILU_ERR_INVALID, "options: bad precond");
+  if (o->ilu_approach < 1 || o->ilu_approach > 4) return set_error(BILU_ERR_INVALID, "options: ilu_approach must be 1..4");
+  if (o->parilu_sweeps < 0) return set_error(BILU_ERR_INVALID, "options: parilu_sweeps < 0");
+  if (o->isai_power < 1) return set_error(BILU_ERR_INVALID, "options: isai_power < 1");
+  if (o->tol_mode != BILU_TOL_ABS && o->tol_mode != BILU_TOL_REL) return set_error(BILU_ERR_INVALID, "options: tol_mode");
+  if (!(o->tol >= 0.0)) return set_error(BILU_ERR_INVALID, "options: tol must be >= 0");
+  if (o->max_iter < 0) return set_error(BILU_ERR_INVALID, "options: max_iter < 0");
+  if (o->factor_precision != BILU_FP64 && o->factor_precision != BILU_FP32)
+    return set_error(BILU_ERR_INVALID, "options: factor_precision");
+  if (o->reduction != BILU_REDUCE_REF && o->reduction != BILU_REDUCE_FAST)
+    return set_error(BILU_ERR_INVALID, "options: reduction");
+  if (o->threads_per_system < 0 || o->threads_per_system > 1024)
+    return set_error(BILU_ERR_INVALID, "options: threads_per_system must be 0..1024");
+  return BILU_OK;
+}
+
+}  // namespace plan_detail
+
+using namespace plan_detail;
+
+// ===========================================================================
+// entry points
+// ===========================================================================
+extern "C" {
+
+void bilu_default_options(bilu_options* o) {
+  if (!o) return;
+  o->precond = BILU_PRECOND_ILU0;
+  o->ilu_approach = 1;
+  o->parilu_sweeps = 5;
+  o->isai_power = 2;
+  o->tol_mode = BILU_TOL_ABS;
+  o->tol = 1e-11;
+  o->max_iter = 500;
+  o->factor_precision = BILU_FP64;
+  o->reduction = BILU_REDUCE_REF;
+  o->compute_true_residual = 1;
+  o->threads_per_system = 0;
+}
+
+const char* bilu_last_error(void) { return g_last_error.c_str(); }
+const char* bilu_version(void) { return "bilu 0.1 (sm_103a)"; }
+
+int bilu_device_count(void) {
+  int c = 0;
+  if (cudaGetDeviceCount(&c) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return c;
+}
+
+bilu_status bilu_plan_create(bilu_plan** out, int n, int nnz, const int* h_rp, const int* h_ci,
+                             const bilu_options* opts) {
+  if (!out) return set_error(BILU_ERR_INVALID, "bilu_plan_create: out is NULL");
+  *out = nullptr;
+  if (n <= 0 || nnz < 0 || !h_rp || (nnz > 0 && !h_ci)) return set_error(BILU_ERR_INVALID, "bilu_plan_create: bad sizes");
+  bilu_status st = check_opts(opts);
+  if (st) return st;
+  // validate CSR
+  if (h_rp[0] != 0 || h_rp[n] != nnz) return set_error(BILU_ERR_PATTERN, "row pointers must start at 0 and end at nnz");
+  for (int i = 0; i < n; ++i) {
+    if (h_rp[i + 1] < h_rp[i]) return set_error(BILU_ERR_PATTERN, "row pointers decrease at row " + std::to_string(i));
+    for (int k = h_rp[i]; k < h_rp[i + 1]; ++k) {
+      if (h_ci[k] < 0 || h_ci[k] >= n)
+        return set_error(BILU_ERR_PATTERN, "column index out of range in row " + std::to_string(i));
+      if (k > h_rp[i] && h_ci[k] <= h_ci[k - 1])
+        return set_error(BILU_ERR_PATTERN, "columns not strictly ascending in row " + std::to_string(i));
+    }
+  }
+  if (bilu_device_count() == 0) return set_error(BILU_ERR_NO_DEVICE, "no CUDA device");
+  bilu_plan* P = new bilu_plan();
+  if (opts)
+    P->opts = *opts;
+  else
+    bilu_default_options(&P->opts);
+  cudaGetDevice(&P->device);
+  P->n = n;
+  P->nnz_in = nnz;
+  P->in_rp.assign(h_rp, h_rp + n + 1);
+  P->in_ci.assign(h_ci, h_ci + nnz);
+  // missing diagonals (Count/Add_Missing_Diagonal_Elements, factorization.cu:399-467)
+  P->rp.assign(n + 1, 0);
+  P->ci.clear();
+  P->src.clear();
+  for (int i = 0; i < n; ++i) {
+    bool has = false;
+    for (int k = h_rp[i]; k < h_rp[i + 1]; ++k) has |= (h_ci[k] == i);
+    bool placed = has;
+    if (!has) P->missing++;
+    for (int k = h_rp[i]; k < h_rp[i + 1]; ++k) {
+      if (!placed && h_ci[k] > i) {
+        P->ci.push_back(i);
+        P->src.push_back(-1);
+        placed = true;
+      }
+      P->ci.push_back(h_ci[k]);
+      P->src.push_back(k);
+    }
+    if (!placed) {
+      P->ci.push_back(i);
+      P->src.push_back(-1);
+    }
+    P->rp[i + 1] = (int)P->ci.size();
+  }
+  P->nnz = (int)P->ci.size();
+  if (P->missing > 0 && P->opts.precond == BILU_PRECOND_ILU0) {
+    delete P;
+    return set_error(BILU_ERR_PATTERN,
+                     "the merged ILU(0) solver requires every diagonal entry in the pattern (as the reference's "
+                     "merged solver, which asserts); use BILU_PRECOND_ILU0_SPLIT");
+  }
+  P->diag.assign(n, -1);
+  P->row_of.assign(P->nnz, 0);
+  for (int i = 0; i < n; ++i)
+    for (int k = P->rp[i]; k < P->rp[i + 1]; ++k) {
+      P->row_of[k] = i;
+      if (P->ci[k] == i) P->diag[i] = k;
+      P->maxl = std::max(P->maxl, P->rp[i + 1] - P->rp[i]);
+    }
+  for (int i = 0; i < n; ++i) P->a_maxl = std::max(P->a_maxl, h_rp[i + 1] - h_rp[i]);
+  // L / U split (factorization.cu:216-344)
+  P->l_rp.assign(n + 1, 0);
+  P->u_rp.assign(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    for (int k = P->rp[i]; k < P->diag[i]; ++k) {
+      P->l_ci.push_back(P->ci[k]);
+      P->l_src.push_back(k);
+    }
+    P->l_ci.push_back(i);
+    P->l_src.push_back(-1);
+    for (int k = P->diag[i]; k < P->rp[i + 1]; ++k) {
+      P->u_ci.push_back(P->ci[k]);
+      P->u_src.push_back(k);
+    }
+    P->l_rp[i + 1] = (int)P->l_ci.size();
+    P->u_rp[i + 1] = (int)P->u_ci.size();
+  }
+  build_levels(*P);
+  build_deps(*P);
+  P->has_isai = is_isai(P->opts.precond);
+  if (P->has_isai) {
+    st = build_isai(*P);
+    if (st) {
+      delete P;
+      return st;
+    }
+  }
+  choose_layout(*P);
+  if (P->lay.total > (int)solve_max_smem()) {
+    const int need = P->lay.total;
+    delete P;
+    return set_error(BILU_ERR_CAPACITY, "solver needs " + std::to_string(need) + " bytes of shared memory per system");
+  }
+  st = upload(*P);
+  if (st) {
+    if (P->dbuf) cudaFree(P->dbuf);
+    delete P;
+    return st;
+  }
+  *out = P;
+  return BILU_OK;
+}
+
+bilu_status bilu_plan_enable_timing(bilu_plan* P, int enable) {
+  if (!P) return set_error(BILU_ERR_INVALID, "bilu_plan_enable_timing: NULL plan");
+  if (enable && !P->ev[0]) {
+    for (auto& e : P->ev) {
+      cudaError_t r = cudaEventCreate(&e);
+      if (r != cudaSuccess) return cuda_err(r, "cudaEventCreate");
+    }
+  }
+  P->timing = enable != 0;
+  return BILU_OK;
+}
+
+bilu_status bilu_plan_last_timing(bilu_plan* P, bilu_timing* t) {
+  if (!P || !t) return set_error(BILU_ERR_INVALID, "bilu_plan_last_timing: NULL argument");
+  if (!P->timing) return set_error(BILU_ERR_INVALID, "bilu_plan_last_timing: timing not enabled");
+  cudaError_t r = cudaEventSynchronize(P->ev[2]);
+  if (r != cudaSuccess) return cuda_err(r, "cudaEventSynchronize");
+  cudaEventElapsedTime(&t->setup_ms, P->ev[0], P->ev[1]);
+  cudaEventElapsedTime(&t->solve_ms, P->ev[1], P->ev[2]);
+  cudaEventElapsedTime(&t->total_ms, P->ev[0], P->ev[2]);
+  return BILU_OK;
+}
+
+bilu_status bilu_plan_destroy(bilu_plan* P) {
+  if (!P) return BILU_OK;
+  for (auto& e : P->ev)
+    if (e) cudaEventDestroy(e);
+  if (P->dbuf) cudaFree(P->dbuf);
+  if (P->ws) cudaFree(P->ws);
+  delete P;
+  return BILU_OK;
+}
+
+bilu_status bilu_plan_get_info(const bilu_plan* P, bilu_plan_info* info) {
+  if (!P || !info) return set_error(BILU_ERR_INVALID, "bilu_plan_get_info: NULL argument");
+  info->n = P->n;
+  info->nnz = P->nnz;
+  info->nnz_in = P->nnz_in;
+  info->missing_diag = P->missing;
+  info->nnz_L = (int)P->l_src.size();
+  info->nnz_U = (int)P->u_src.size();
+  info->nnz_isai_L = P->has_isai ? P->ail_rp[P->n] : 0;
+  info->nnz_isai_U = P->has_isai ? P->aiu_rp[P->n] : 0;
+  info->levels_lower = (int)P->lev_lo_ptr.size() - 1;
+  info->levels_upper = (int)P->lev_up_ptr.size() - 1;
+  info->max_row_len = P->maxl;
+  info->threads = P->threads;
+  info->smem_bytes = P->lay.total;
+  info->operands_in_smem = (P->lay.A >= 0 ? 1 : 0) | ((P->lay.F >= 0 || P->lay.ail >= 0) ? 2 : 0) |
+                           (P->lay.aiu >= 0 ? 4 : 0);
+  return BILU_OK;
+}
+
+bilu_status bilu_plan_get_pattern(const bilu_plan* P, int which, int* n, int* nnz, int* h_rp, int* h_ci) {
+  if (!P) return set_error(BILU_ERR_INVALID, "bilu_plan_get_pattern: NULL plan");
+  const std::vector<int>* rp = nullptr;
+  const std::vector<int>* ci = nullptr;
+  switch (which) {
+    case 0: rp = &P->rp; ci = &P->ci; break;
+    case 1: rp = &P->ail_rp; ci = &P->ail_ci; break;
+    case 2: rp = &P->aiu_rp; ci = &P->aiu_ci; break;
+    case 3: rp = &P->l_rp; ci = &P->l_ci; break;
+    case 4: rp = &P->u_rp; ci = &P->u_ci; break;
+    default: return set_error(BILU_ERR_INVALID, "bilu_plan_get_pattern: which must be 0..4");
+  }
+  if ((which == 1 || which == 2) && !P->has_isai)
+    return set_error(BILU_ERR_INVALID, "bilu_plan_get_pattern: the plan has no ISAI pattern");
+  if (n) *n = P->n;
+  if (nnz) *nnz = rp->empty() ? 0 : rp->back();
+  if (h_rp) std::memcpy(h_rp, rp->data(), sizeof(int) * rp->size());
+  if (h_ci && !ci->empty()) std::memcpy(h_ci, ci->data(), sizeof(int) * ci->size());
+  return BILU_OK;
+}
+
+bilu_status bilu_expand_values(const bilu_plan* P, int nsys, const double* vin, double* vout, void* stream) {
+  if (!P || nsys < 0 || (nsys > 0 && (!vin || !vout))) return set_error(BILU_ERR_INVALID, "bilu_expand_values: bad args");
+  cudaError_t e = launch_expand(P->dp, nsys, vin, vout, (cudaStream_t)stream);
+  return e == cudaSuccess ? BILU_OK : cuda_err(e, "expand");
+}
+
+}  // extern "C"
+
+namespace plan_detail {
+
+// factor-pattern values for the factorisation kernels: the caller's array
+// when no diagonal was inserted, else an expanded copy in `scratch`
+const double* factor_values(bilu_plan* P, int nsys, const double* vin, double* scratch, cudaStream_t st,
+                            cudaError_t* err) {
+  *err = cudaSuccess;
+  if (P->missing == 0) return vin;
+  *err = launch_expand(P->dp, nsys, vin, scratch, st);
+  return scratch;
+}
+
+int fact_threads(const bilu_plan* P) { return std::min(512, round_up(std::max(P->n, 64), 32)); }
+
+bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double* lu_init, const double* b, double* x,
+                       const bilu_results* R, cudaStream_t st) {
+  if (nsys < 0 || (nsys > 0 && (!vals || !b || !x))) return set_error(BILU_ERR_INVALID, "bilu_solve: bad arguments");
+  if (nsys == 0) return BILU_OK;
+  const bilu_options& o = P->opts;
+  const bool fp32 = is_fp32(o);
+  const size_t nz = (size_t)P->nnz * nsys;
+  // workspace: [expanded values][LU][LU float | aiL][aiU]
+  size_t need = 0;
+  const size_t off_exp = need;
+  if (P->missing) need += align_up(nz * 8);
+  const size_t off_lu = need;
+  need += align_up(nz * 8);
+  const size_t off_f = need;
+  if (fp32) need += align_up(nz * 4);
+  const size_t off_ail = need;
+  if (P->has_isai) need += align_up((size_t)P->dp.ail_nnz * nsys * 8);
+  const size_t off_aiu = need;
+  if (P->has_isai) need += align_up((size_t)P->dp.aiu_nnz * nsys * 8);
+  const int prec = o.precond;
+  if (P->timing) cudaEventRecord(P->ev[0], st);
+  if (prec != BILU_PRECOND_ILU0 && prec != BILU_PRECOND_NONE) {
+    bilu_status s = ensure_ws(P, need);
+    if (s) return s;
+  }
+  char* ws = (char*)P->ws;
+  SolveArgs a;
+  a.pat = P->dp;
+  a.lay = P->lay;
+  a.nsys = nsys;
+  a.A = vals;
+  a.b = b;
+  a.x = x;
+  if (R) {
+    a.iters = R->iter_counts;
+    a.conv = R->conv_flags;
+    a.res = R->iter_res_norms;
+    a.status = R->status;
+    a.true_res = o.compute_true_residual ? R->true_res_norms : nullptr;
+  }
+  a.tol = o.tol;
+  a.tol_mode = o.tol_mode;
+  a.max_iter = o.max_iter;
+  a.approach = o.ilu_approach;
+  a.dot_serial = is_isai(prec) ? 1 : 0;
+  cudaError_t e = cudaSuccess;
+  const int ft = fact_threads(P);
+  if (prec == BILU_PRECOND_ILU0) {
+    a.prec = PK_ILU_INKERNEL;
+  } else if (prec == BILU_PRECOND_NONE) {
+    a.prec = PK_NONE;
+  } else {
+    const double* fv = factor_values(P, nsys, vals, (double*)(ws + off_exp), st, &e);
+    if (e != cudaSuccess) return cuda_err(e, "expand");
+    double* lu = (double*)(ws + off_lu);
+    if (prec == BILU_PRECOND_ILU0_SPLIT || prec == BILU_PRECOND_ILU0_ISAI)
+      e = launch_ilu0(P->dp, nsys, fv, lu, o.ilu_approach, ft, st);
+    else
+      e = launch_parilu0(P->dp, nsys, fv, lu_init, lu, o.parilu_sweeps, ft, st);
+    if (e != cudaSuccess) return cuda_err(e, "factorisation");
+    if (is_isai(prec)) {
+      void* ail = ws + off_ail;
+      void* aiu = ws + off_aiu;
+      e = launch_isai(P->dp, nsys, lu, ail, aiu, fp32 ? 1 : 0, ft, st);
+      if (e != cudaSuccess) return cuda_err(e, "isai");
+      a.prec = PK_ISAI;
+      a.ail = ail;
+      a.aiu = aiu;
+    } else {
+      a.prec = PK_LU_GLOBAL;
+      if (fp32) {
+        float* f = (float*)(ws + off_f);
+        e = launch_to_float(lu, f, nz, st);
+        if (e != cudaSuccess) return cuda_err(e, "convert");
+        a.F = f;
+      } else {
+        a.F = lu;
+      }
+    }
+  }
+  int maxl = P->a_maxl;
+  if (P->has_isai) {
+    for (int i = 0; i < P->n; ++i) {
+      maxl = std::max(maxl, P->ail_rp[i + 1] - P->ail_rp[i]);
+      maxl = std::max(maxl, P->aiu_rp[i + 1] - P->aiu_rp[i]);
+    }
+  }
+  if (P->timing) cudaEventRecord(P->ev[1], st);
+  e = launch_solve(a, P->threads, fp32 ? 1 : 0, o.reduction == BILU_REDUCE_FAST ? 1 : 0, maxl, st);
+  if (e != cudaSuccess) return cuda_err(e, "solver launch");
+  if (P->timing) cudaEventRecord(P->ev[2], st);
+  return BILU_OK;
+}
+
+}  // namespace plan_detail
+
+extern "C" {
+
+bilu_status bilu_solve(bilu_plan* P, int nsys, const double* d_values, const double* d_b, double* d_x,
+                       const bilu_results* R, void* stream) {
+  if (!P) return set_error(BILU_ERR_INVALID, "bilu_solve: NULL plan");
+  return solve_impl(P, nsys, d_values, nullptr, d_b, d_x, R, (cudaStream_t)stream);
+}
+
+bilu_status bilu_solve_warm(bilu_plan* P, int nsys, const double* d_values, const double* d_lu_init,
+                            const double* d_b, double* d_x, const bilu_results* R, void* stream) {
+  if (!P) return set_error(BILU_ERR_INVALID, "bilu_solve_warm: NULL plan");
+  if (P->opts.precond != BILU_PRECOND_PARILU0 && P->opts.precond != BILU_PRECOND_PARILU0_ISAI)
+    return set_error(BILU_ERR_INVALID, "bilu_solve_warm: only for ParILU preconditioners");
+  return solve_impl(P, nsys, d_values, d_lu_init, d_b, d_x, R, (cudaStream_t)stream);
+}
+
+bilu_status bilu_ilu0(const bilu_plan* Pc, int nsys, const double* d_values, double* d_lu, int approach,
+                      void* stream) {
+  bilu_plan* P = const_cast<bilu_plan*>(Pc);
+  if (!P || nsys < 0 || (nsys > 0 && (!d_values || !d_lu)) || approach < 1 || approach > 4)
+    return set_error(BILU_ERR_INVALID, "bilu_ilu0: bad arguments");
+  if (nsys == 0) return BILU_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const double* fv = d_values;
+  cudaError_t e;
+  if (P->missing) {  // expand straight into the output, factorise in place
+    e = launch_expand(P->dp, nsys, d_values, d_lu, st);
+    if (e != cudaSuccess) return cuda_err(e, "expand");
+    fv = d_lu;
+  }
+  e = launch_ilu0(P->dp, nsys, fv, d_lu, approach, fact_threads(P), st);
+  return e == cudaSuccess ? BILU_OK : cuda_err(e, "ilu0");
+}
+
+bilu_status bilu_parilu0(const bilu_plan* Pc, int nsys, const double* d_values, const double* d_lu_init, double* d_lu,
+                         int sweeps, void* stream) {
+  bilu_plan* P = const_cast<bilu_plan*>(Pc);
+  if (!P || nsys < 0 || sweeps < 0 || (nsys > 0 && (!d_values || !d_lu)))
+    return set_error(BILU_ERR_INVALID, "bilu_parilu0: bad arguments");
+  if (nsys == 0) return BILU_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const double* fv = d_values;
+  if (P->missing) {
+    bilu_status s = ensure_ws(P, align_up((size_t)P->nnz * nsys * 8));
+    if (s) return s;
+    cudaError_t e = launch_expand(P->dp, nsys, d_values, (double*)P->ws, st);
+    if (e != cudaSuccess) return cuda_err(e, "expand");
+    fv = (const double*)P->ws;
+  }
+  cudaError_t e = launch_parilu0(P->dp, nsys, fv, d_lu_init, d_lu, sweeps, fact_threads(P), st);
+  return e == cudaSuccess ? BILU_OK : cuda_err(e, "parilu0");
+}
+
+bilu_status bilu_split_lu(const bilu_plan* P, int nsys, const double* d_lu, double* d_L, double* d_U, void* stream) {
+  if (!P || nsys < 0 || (nsys > 0 && (!d_lu || !d_L || !d_U))) return set_error(BILU_ERR_INVALID, "bilu_split_lu: bad args");
+  cudaError_t e = launch_split(P->dp, nsys, d_lu, d_L, d_U, (cudaStream_t)stream);
+  return e == cudaSuccess ? BILU_OK : cuda_err(e, "split");
+}
+
+bilu_status bilu_isai(const bilu_plan* P, int nsys, const double* d_lu, double* d_ail, double* d_aiu, void* stream) {
+  if (!P || nsys < 0 || (nsys > 0 && (!d_lu || !d_ail || !d_aiu))) return set_error(BILU_ERR_INVALID, "bilu_isai: bad args");
+  if (!P->has_isai) return set_error(BILU_ERR_INVALID, "bilu_isai: plan was not created with an ISAI preconditioner");
+  cudaError_t e = launch_isai(P->dp, nsys, d_lu, d_ail, d_aiu, 0, fact_threads(P), (cudaStream_t)stream);
+  return e == cudaSuccess ? BILU_OK : cuda_err(e, "isai");
+}
+
+bilu_status bilu_true_residual(const bilu_plan* P, int nsys, const double* d_values, const double* d_b,
+                               const double* d_x, double* d_norms, void* stream) {
+  if (!P || nsys < 0 || (nsys > 0 && (!d_values || !d_b || !d_x || !d_norms)))
+    return set_error(BILU_ERR_INVALID, "bilu_true_residual: bad args");
+  // the operator pattern is the caller's pattern
+  DevPattern d = P->dp;
+  d.rp = d.a_rp;
+  d.ci = d.a_ci;
+  d.nnz = d.a_nnz;
+  cudaError_t e = launch_true_residual(d, nsys, d_values, d_b, d_x, d_norms, 256, (cudaStream_t)stream);
+  return e == cudaSuccess ? BILU_OK : cuda_err(e, "true residual");
+}
+
+}  // extern "C"

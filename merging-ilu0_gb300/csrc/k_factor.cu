@@ -1,0 +1,320 @@
+// Preconditioner-generation kernels: ILU(0) (all four reference approaches'
+// arithmetic), ParILU(0) Jacobi sweeps, ISAI of L and U, the reference's L/U
+// split, missing-diagonal value scatter and the true-residual kernel.  One
+// CTA per system, the system's values staged in shared memory.
+//
+// Reference (paths inside Batched-ILU0-merged/ILU0_ISAI_bicgstab/):
+//   ILU(0)      ILU_0_gpu.cu:26-186 (approach 1), :376-685 (2), :693-935 (3), :947-1229 (4)
+//   ParILU(0)   parILU_0_gpu.cu:18-113, dependency list :118-220
+//   ISAI        isai_gpu.cu:209-287 (extraction), :325-389 (triangular solves), :559-626
+//   L/U split   factorization.cu:216-344
+//   diag add    factorization.cu:169-188
+//   true res.   Bicgstab_common.hpp:294-342
+#include <cuda_runtime.h>
+
+#include "bilu_internal.h"
+
+namespace bilu {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------- value scatter
+__global__ void k_expand(const int* __restrict__ src, int nnz, int nnz_in, int nsys, const double* __restrict__ vin,
+                         double* __restrict__ vout) {
+  const size_t total = (size_t)nnz * nsys;
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < total; g += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(g % nnz);
+    const size_t s = g / nnz;
+    const int sidx = __ldg(src + k);
+    vout[g] = sidx < 0 ? 0.0 : __ldg(vin + s * nnz_in + sidx);
+  }
+}
+
+// ---------------------------------------------------------------- ILU(0)
+// Same per-entry arithmetic as the solver kernel's in-kernel factorisation.
+__global__ void __launch_bounds__(512) k_ilu0(const DevPattern P, int nsys, const double* __restrict__ A,
+                                              double* __restrict__ LUout, int approach) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sys = blockIdx.x;
+  if (sys >= nsys) return;
+  const int nnz = P.nnz;
+  double* LU = reinterpret_cast<double*>(smem);
+  for (int k = threadIdx.x; k < nnz; k += blockDim.x) LU[k] = __ldg(A + (size_t)sys * nnz + k);
+  __syncthreads();
+  for (int lev = 0; lev < P.nlev_lo; ++lev) {
+    const int b = __ldg(P.lev_lo_ptr + lev), e = __ldg(P.lev_lo_ptr + lev + 1);
+    for (int q = b + threadIdx.x; q < e; q += blockDim.x) {
+      const int i = __ldg(P.lev_lo_rows + q);
+      const int rb = __ldg(P.rp + i), re = __ldg(P.rp + i + 1);
+      for (int k = rb; k < re; ++k) {
+        const int j = __ldg(P.ci + k);
+        const int pb = __ldg(P.dep_ptr + k), pe = __ldg(P.dep_ptr + k + 1);
+        double v;
+        if (approach == 1 || approach == 4) {
+          v = LU[k];
+          for (int q2 = pb; q2 < pe; ++q2) {
+            const int2 d = __ldg(P.dep + q2);
+            v = fma(-LU[d.x], LU[d.y], v);
+          }
+        } else {
+          double s = 0.0;
+          if (approach == 3) {
+            for (int q2 = pb; q2 < pe; ++q2) {
+              const int2 d = __ldg(P.dep + q2);
+              s = fma(LU[d.x], LU[d.y], s);
+            }
+          } else {
+            for (int q2 = pe - 1; q2 >= pb; --q2) {
+              const int2 d = __ldg(P.dep + q2);
+              s = fma(LU[d.y], LU[d.x], s);
+            }
+          }
+          v = LU[k] - s;
+        }
+        if (j < i) v = v / LU[__ldg(P.diag + j)];
+        LU[k] = v;
+      }
+    }
+    __syncthreads();
+  }
+  for (int k = threadIdx.x; k < nnz; k += blockDim.x) LUout[(size_t)sys * nnz + k] = LU[k];
+}
+
+// ---------------------------------------------------------------- ParILU(0)
+// Jacobi sweeps: every entry of sweep t+1 is computed from the values of
+// sweep t (parilu0_sweep_for_batch_entry_approach2's formula,
+// parILU_0_gpu.cu:18-57: sum of l_ik*u_kj by fma from 0 in ascending k, then
+// (a_ij - sum)/u_jj below the diagonal, (a_ij - sum)/1 elsewhere).
+__global__ void __launch_bounds__(512) k_parilu0(const DevPattern P, int nsys, const double* __restrict__ A,
+                                                 const double* __restrict__ init, double* __restrict__ LUout,
+                                                 int sweeps) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sys = blockIdx.x;
+  if (sys >= nsys) return;
+  const int nnz = P.nnz;
+  double* As = reinterpret_cast<double*>(smem);
+  double* cur = As + nnz;
+  double* nxt = cur + nnz;
+  const double* Ag = A + (size_t)sys * nnz;
+  const double* Ig = init ? init + (size_t)sys * nnz : Ag;
+  for (int k = threadIdx.x; k < nnz; k += blockDim.x) {
+    As[k] = __ldg(Ag + k);
+    cur[k] = __ldg(Ig + k);
+  }
+  __syncthreads();
+  for (int it = 0; it < sweeps; ++it) {
+    for (int k = threadIdx.x; k < nnz; k += blockDim.x) {
+      const int pb = __ldg(P.dep_ptr + k), pe = __ldg(P.dep_ptr + k + 1);
+      double s = 0.0;
+      for (int q = pb; q < pe; ++q) {
+        const int2 d = __ldg(P.dep + q);
+        s = fma(cur[d.x], cur[d.y], s);
+      }
+      double v = As[k] - s;
+      const int i = __ldg(P.row_of + k), j = __ldg(P.ci + k);
+      if (j < i) v = v / cur[__ldg(P.diag + j)];
+      nxt[k] = v;
+    }
+    __syncthreads();
+    double* tswap = cur;
+    cur = nxt;
+    nxt = tswap;
+  }
+  for (int k = threadIdx.x; k < nnz; k += blockDim.x) LUout[(size_t)sys * nnz + k] = cur[k];
+}
+
+// ---------------------------------------------------------------- ISAI
+// One thread per ISAI row.  For row i with pattern J (|J| = sz <= 32) the
+// reference solves T(J,J)^T m = e_pos with one warp lane per unknown
+// (isai_gpu.cu:325-389); the same operations in the same order per unknown:
+//   L (lower, unit diagonal): m_{sz-1} = 1; for t = sz-2..0:
+//        acc = 0; for c = sz-1..t+1: acc = fma(-m_c, L(J_c,J_t), acc); m_t = acc / 1
+//   U (upper): m_0 = 1 / u_ii; for t = 1..sz-1:
+//        acc = 0; for c = 0..t-1: acc = fma(-m_c, U(J_c,J_t), acc); m_t = acc / U(J_t,J_t)
+// The per-row program lists the structurally nonzero (c, position) pairs in
+// exactly that order (zeros of T(J,J) give exact no-op updates).  m is
+// accumulated in FP64 in shared memory and rounded to FT on the way out.
+template <typename FT>
+__global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, const double* __restrict__ LUg,
+                                              FT* __restrict__ ail, FT* __restrict__ aiu) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sys = blockIdx.x;
+  if (sys >= nsys) return;
+  const int n = P.n, nnz = P.nnz;
+  double* LU = reinterpret_cast<double*>(smem);
+  double* M = LU + nnz;  // max(ail_nnz, aiu_nnz)
+  for (int k = threadIdx.x; k < nnz; k += blockDim.x) LU[k] = __ldg(LUg + (size_t)sys * nnz + k);
+  __syncthreads();
+  // ---- aiL
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int beg = __ldg(P.ail_rp + i), sz = __ldg(P.ail_rp + i + 1) - beg;
+    double* m = M + beg;
+    m[sz - 1] = 1.0;
+    int q = __ldg(P.ail_prog_ptr + i);
+    for (int blk = 0; blk < sz - 1; ++blk) {
+      const int2 h = __ldg(P.ail_prog + q++);  // {t, count}
+      double acc = 0.0;
+      for (int u = 0; u < h.y; ++u) {
+        const int2 e = __ldg(P.ail_prog + q++);  // {c, position in LU}
+        acc = fma(-m[e.x], LU[e.y], acc);
+      }
+      m[h.x] = acc;
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < P.ail_nnz; k += blockDim.x) ail[(size_t)sys * P.ail_nnz + k] = (FT)M[k];
+  __syncthreads();
+  // ---- aiU
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int beg = __ldg(P.aiu_rp + i), sz = __ldg(P.aiu_rp + i + 1) - beg;
+    double* m = M + beg;
+    m[0] = 1.0 / LU[__ldg(P.diag + i)];
+    int q = __ldg(P.aiu_prog_ptr + i);
+    for (int blk = 1; blk < sz; ++blk) {
+      const int2 h = __ldg(P.aiu_prog + q++);
+      double acc = 0.0;
+      for (int u = 0; u < h.y; ++u) {
+        const int2 e = __ldg(P.aiu_prog + q++);
+        acc = fma(-m[e.x], LU[e.y], acc);
+      }
+      const int jt = __ldg(P.aiu_ci + beg + h.x);
+      m[h.x] = acc / LU[__ldg(P.diag + jt)];
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < P.aiu_nnz; k += blockDim.x) aiu[(size_t)sys * P.aiu_nnz + k] = (FT)M[k];
+}
+
+// ---------------------------------------------------------------- L / U split
+__global__ void k_split(const DevPattern P, int nsys, const double* __restrict__ LU, double* __restrict__ L,
+                        double* __restrict__ U) {
+  const size_t totL = (size_t)P.nnz_L * nsys, totU = (size_t)P.nnz_U * nsys;
+  const size_t tot = totL > totU ? totL : totU;
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < tot; g += (size_t)gridDim.x * blockDim.x) {
+    if (g < totL) {
+      const int k = (int)(g % P.nnz_L);
+      const size_t s = g / P.nnz_L;
+      const int src = __ldg(P.l_src + k);
+      L[g] = src < 0 ? 1.0 : __ldg(LU + s * P.nnz + src);
+    }
+    if (g < totU) {
+      const int k = (int)(g % P.nnz_U);
+      const size_t s = g / P.nnz_U;
+      U[g] = __ldg(LU + s * P.nnz + __ldg(P.u_src + k));
+    }
+  }
+}
+
+// ---------------------------------------------------------------- true residual
+// One warp per system: rows in the SpMV tree order of the reference
+// (ComputeResidualVec, warp per row), norm = sqrt of the serial inner product
+// (L2Norm(n, v), Bicgstab_common.hpp:132) accumulated by lane 0.
+__global__ void k_true_residual(const DevPattern P, int nsys, const double* __restrict__ A,
+                                const double* __restrict__ b, const double* __restrict__ x, double* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sys = blockIdx.x;
+  if (sys >= nsys) return;
+  const int n = P.n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  double* rs = reinterpret_cast<double*>(smem);
+  const double* As = A + (size_t)sys * P.nnz;
+  const double* xs = x + (size_t)sys * n;
+  const double* bs = b + (size_t)sys * n;
+  for (int i = warp; i < n; i += nw) {
+    const int beg = __ldg(P.rp + i), end = __ldg(P.rp + i + 1);
+    double t = 0.0;
+    for (int k = beg + lane; k < end; k += 32) t = fma(__ldg(As + k), __ldg(xs + __ldg(P.ci + k)), t);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(kFull, t, off);
+    if (lane == 0) rs[i] = __ldg(bs + i) - t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double acc = 0.0;
+    for (int i = 0; i < n; ++i) acc = fma(rs[i], rs[i], acc);
+    out[sys] = sqrt(acc);
+  }
+}
+
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+int grid_for(size_t total, int threads) {
+  size_t g = (total + threads - 1) / threads;
+  if (g > 65536) g = 65536;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+}  // namespace
+
+cudaError_t launch_expand(const DevPattern& p, int nsys, const double* vin, double* vout, cudaStream_t st) {
+  if (nsys == 0) return cudaSuccess;
+  k_expand<<<grid_for((size_t)p.nnz * nsys, 256), 256, 0, st>>>(p.src_map, p.nnz, p.nnz_in, nsys, vin, vout);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ilu0(const DevPattern& p, int nsys, const double* A, double* lu, int approach, int threads,
+                        cudaStream_t st) {
+  if (nsys == 0) return cudaSuccess;
+  const int smem = p.nnz * 8;
+  cudaError_t e = cudaFuncSetAttribute(k_ilu0, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_ilu0<<<nsys, threads, smem, st>>>(p, nsys, A, lu, approach);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_parilu0(const DevPattern& p, int nsys, const double* A, const double* init, double* lu,
+                           int sweeps, int threads, cudaStream_t st) {
+  if (nsys == 0) return cudaSuccess;
+  const int smem = p.nnz * 8 * 3;
+  cudaError_t e = cudaFuncSetAttribute(k_parilu0, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_parilu0<<<nsys, threads, smem, st>>>(p, nsys, A, init, lu, sweeps);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_isai(const DevPattern& p, int nsys, const double* lu, void* ail, void* aiu, int fp32, int threads,
+                        cudaStream_t st) {
+  if (nsys == 0) return cudaSuccess;
+  const int smem = (p.nnz + (p.ail_nnz > p.aiu_nnz ? p.ail_nnz : p.aiu_nnz)) * 8;
+  cudaError_t e;
+  if (fp32) {
+    e = cudaFuncSetAttribute(k_isai<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_isai<float><<<nsys, threads, smem, st>>>(p, nsys, lu, (float*)ail, (float*)aiu);
+  } else {
+    e = cudaFuncSetAttribute(k_isai<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_isai<double><<<nsys, threads, smem, st>>>(p, nsys, lu, (double*)ail, (double*)aiu);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_float(const double* a, float* b, size_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_to_float<<<grid_for(n, 256), 256, 0, st>>>(a, b, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_split(const DevPattern& p, int nsys, const double* lu, double* L, double* U, cudaStream_t st) {
+  if (nsys == 0) return cudaSuccess;
+  const size_t tot = (size_t)(p.nnz_L > p.nnz_U ? p.nnz_L : p.nnz_U) * nsys;
+  k_split<<<grid_for(tot, 256), 256, 0, st>>>(p, nsys, lu, L, U);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_true_residual(const DevPattern& p, int nsys, const double* A, const double* b, const double* x,
+                                 double* out, int threads, cudaStream_t st) {
+  if (nsys == 0) return cudaSuccess;
+  const int smem = p.n * 8;
+  cudaError_t e = cudaFuncSetAttribute(k_true_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_true_residual<<<nsys, threads, smem, st>>>(p, nsys, A, b, x, out);
+  return cudaGetLastError();
+}
+
+}  // namespace bilu

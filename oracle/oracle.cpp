@@ -1,0 +1,673 @@
+// ORACLE -- test infrastructure only.
+//
+// CPU restatement of the reference's batched ILU(0) / ParILU(0) / ISAI /
+// BiCGSTAB arithmetic (aggarwal2000/Merging-ILU0, paths relative to
+// Batched-ILU0-merged/ILU0_ISAI_bicgstab/).  Every floating-point operation is
+// written out in the order the reference's CUDA kernels perform it, with the
+// fused multiply-adds that nvcc contracts `a += b*c` / `a - b*c` into made
+// explicit (std::fma); the file is compiled with -ffp-contract=off so the host
+// compiler adds no contraction of its own.  The reference kernels themselves
+// are compiled from source and run on the GPU by oracle/ref_launch.cpp, which
+// is what pins this restatement (tests/test_ref_pin.py).
+//
+// Only tests, the smoke check and bench.py's CPU-baseline leg may call this
+// library; the product path (libbilu) never links or loads it.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_API extern "C" __attribute__((visibility("default")))
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// reductions in the reference's order
+// ---------------------------------------------------------------------------
+
+// inner_product(n, v1, v2, result) (Bicgstab_common.hpp:97-128): warp 0 only,
+// lane l accumulates idx = l, l+32, ... with `temp += v1*v2` (fma), then a
+// __shfl_down_sync tree with offsets 16, 8, 4, 2, 1; lane 0 holds the result.
+inline double dot_warp0(int n, const double* a, const double* b) {
+  double p[32];
+  for (int l = 0; l < 32; ++l) {
+    double t = 0.0;
+    for (int i = l; i < n; i += 32) t = std::fma(a[i], b[i], t);
+    p[l] = t;
+  }
+  for (int off = 16; off > 0; off >>= 1)
+    for (int l = 0; l < off; ++l) p[l] = p[l] + p[l + off];
+  return p[0];
+}
+
+// inner_product(n, v1, v2) (Bicgstab_common.hpp:82-95): serial loop, every
+// thread computes the same value; used by the ISAI solver kernels.
+inline double dot_serial(int n, const double* a, const double* b) {
+  double t = 0.0;
+  for (int i = 0; i < n; ++i) t = std::fma(a[i], b[i], t);
+  return t;
+}
+
+// One row of SpMV / ComputeResidualVec (Bicgstab_common.hpp:5-40, 254-290):
+// warp per row, lane l accumulates entries beg+l, beg+l+32, ... with
+// `temp += val*vec[col]` (fma), then the 16..1 shfl_down tree.
+inline double row_tree(const double* vals, const int* ci, int beg, int end, const double* x) {
+  double p[32];
+  for (int l = 0; l < 32; ++l) {
+    double t = 0.0;
+    for (int k = beg + l; k < end; k += 32) t = std::fma(vals[k], x[ci[k]], t);
+    p[l] = t;
+  }
+  for (int off = 16; off > 0; off >>= 1)
+    for (int l = 0; l < off; ++l) p[l] = p[l] + p[l + off];
+  return p[0];
+}
+
+inline void spmv_tree(int n, const int* rp, const int* ci, const double* vals, const double* x, double* y) {
+  for (int i = 0; i < n; ++i) y[i] = row_tree(vals, ci, rp[i], rp[i + 1], x);
+}
+
+// FP32-stored ISAI applied in FP32 (the library's BILU_FP32 mode; no
+// reference counterpart): input rounded to float, each row a sequential fmaf
+// sum in CSR order, result widened to double.
+inline void spmv_f32(int n, const int* rp, const int* ci, const float* vals, const float* x, float* y) {
+  for (int i = 0; i < n; ++i) {
+    float acc = 0.0f;
+    for (int k = rp[i]; k < rp[i + 1]; ++k) acc = std::fmaf(vals[k], x[ci[k]], acc);
+    y[i] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// triangular solves on in-place factors (L strictly lower with unit diagonal,
+// U upper), PrecondBiCGSTAB_exact_ilu0_app1_merged_gpu.cu:22-143 and the
+// split L/U form PrecondBiCGSTAB_ilu_gpu.cu:22-150 (same arithmetic: the L
+// diagonal there is an explicit 1.0 and x/1.0 == x).
+// lower: sum over the row's entries left of the diagonal in ascending order
+//        (fma), y_i = (v_i - sum)/1
+// upper: sum over the entries right of the diagonal in DESCENDING order (fma),
+//        z_i = (y_i - sum)/u_ii
+// ---------------------------------------------------------------------------
+inline void trsv_lu(int n, const int* rp, const int* ci, const int* diag, const double* lu, const double* v,
+                    double* y, double* z) {
+  for (int i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int k = rp[i]; k < diag[i]; ++k) s = std::fma(lu[k], y[ci[k]], s);
+    y[i] = v[i] - s;
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = 0.0;
+    for (int k = rp[i + 1] - 1; k > diag[i]; --k) s = std::fma(lu[k], z[ci[k]], s);
+    z[i] = (y[i] - s) / lu[diag[i]];
+  }
+}
+
+// FP32-stored factors, applied in FP32 (the library's BILU_FP32 mode; no
+// reference counterpart): the right-hand side is rounded to float, every
+// product-sum is an fmaf in the same order as above, the diagonal division is
+// a multiplication by the float reciprocal rounded from the double
+// reciprocal, and the result is widened back to double.
+inline void trsv_lu_f32(int n, const int* rp, const int* ci, const int* diag, const float* lu, const float* rinv,
+                        const double* v, float* y, double* z_out) {
+  for (int i = 0; i < n; ++i) {
+    float s = 0.0f;
+    for (int k = rp[i]; k < diag[i]; ++k) s = std::fmaf(lu[k], y[ci[k]], s);
+    y[i] = (float)v[i] - s;
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    float s = 0.0f;
+    for (int k = rp[i + 1] - 1; k > diag[i]; --k) s = std::fmaf(lu[k], y[ci[k]], s);
+    y[i] = (y[i] - s) * rinv[i];
+  }
+  for (int i = 0; i < n; ++i) z_out[i] = (double)y[i];
+}
+
+}  // namespace
+
+// ===========================================================================
+// pattern utilities (factorization.cu)
+// ===========================================================================
+
+// Count_Missing_Diagonal_Elements (factorization.cu:399-421).
+ORC_API int orc_count_missing_diag(int n, const int* rp, const int* ci) {
+  int missing = 0;
+  for (int i = 0; i < n; ++i) {
+    bool has = false;
+    for (int k = rp[i]; k < rp[i + 1]; ++k) has |= (ci[k] == i);
+    missing += has ? 0 : 1;
+  }
+  return missing;
+}
+
+// Add_Missing_Diagonal_Elements (factorization.cu:425-467): the new pattern
+// has (i,i) inserted in column order; src[k_new] = old index or -1 (value 0).
+ORC_API void orc_add_missing_diag(int n, const int* rp, const int* ci, int* new_rp, int* new_ci, int* src) {
+  int pos = 0;
+  new_rp[0] = 0;
+  for (int i = 0; i < n; ++i) {
+    bool has = false;
+    for (int k = rp[i]; k < rp[i + 1]; ++k) has |= (ci[k] == i);
+    bool placed = has;
+    for (int k = rp[i]; k < rp[i + 1]; ++k) {
+      if (!placed && ci[k] > i) {
+        new_ci[pos] = i;
+        src[pos] = -1;
+        ++pos;
+        placed = true;
+      }
+      new_ci[pos] = ci[k];
+      src[pos] = k;
+      ++pos;
+    }
+    if (!placed) {
+      new_ci[pos] = i;
+      src[pos] = -1;
+      ++pos;
+    }
+    new_rp[i + 1] = pos;
+  }
+}
+
+// Find_locations_of_diagonal_elements (factorization.cu:472-480).
+ORC_API void orc_find_diag(int n, const int* rp, const int* ci, int* diag) {
+  for (int i = 0; i < n; ++i) {
+    diag[i] = -1;
+    for (int k = rp[i]; k < rp[i + 1]; ++k)
+      if (ci[k] == i) diag[i] = k;
+  }
+}
+
+// L/U split (factorization.cu:216-344): L row = strictly-lower entries then
+// an explicit unit diagonal; U row = diagonal then the strictly-upper entries.
+// Pattern pass: l_rp/l_ci/u_rp/u_ci; value pass (nsys pages) gathers from the
+// in-place factors.
+ORC_API void orc_split_pattern(int n, const int* rp, const int* ci, const int* diag, int* l_rp, int* l_ci, int* u_rp,
+                               int* u_ci) {
+  l_rp[0] = u_rp[0] = 0;
+  for (int i = 0; i < n; ++i) {
+    int lp = l_rp[i], up = u_rp[i];
+    for (int k = rp[i]; k < diag[i]; ++k) l_ci[lp++] = ci[k];
+    l_ci[lp++] = i;
+    for (int k = diag[i]; k < rp[i + 1]; ++k) u_ci[up++] = ci[k];
+    l_rp[i + 1] = lp;
+    u_rp[i + 1] = up;
+  }
+}
+
+ORC_API void orc_split_values(int n, int nnz, const int* rp, const int* diag, int nsys, const double* lu, int nnz_l,
+                              double* l, int nnz_u, double* u) {
+#pragma omp parallel for schedule(static)
+  for (int s = 0; s < nsys; ++s) {
+    const double* a = lu + (size_t)s * nnz;
+    double* L = l + (size_t)s * nnz_l;
+    double* U = u + (size_t)s * nnz_u;
+    int lp = 0, up = 0;
+    for (int i = 0; i < n; ++i) {
+      for (int k = rp[i]; k < diag[i]; ++k) L[lp++] = a[k];
+      L[lp++] = 1.0;
+      for (int k = diag[i]; k < rp[i + 1]; ++k) U[up++] = a[k];
+    }
+  }
+}
+
+// ===========================================================================
+// ILU(0)
+// ===========================================================================
+//
+// approach 1 (ILU_0_gpu.cu:26-171; the merged solver's inlined copy
+// PrecondBiCGSTAB_exact_ilu0_app1_merged_gpu.cu:145-246): right-looking, for
+// pivot row k = 0..n-1 and every row i > k: l_ik = a_ik / u_kk, then
+// a_ij = fma(-l_ik, u_kj, a_ij) for j > k (rows without a_ik and columns
+// without u_kj receive an exact zero update).  Written here in the same
+// per-entry order: every entry receives its updates in ascending k.
+// approach 4 (ILU_0_gpu.cu:947-1229): the same updates per entry in
+// ascending k (`values[loc] -= values[loc_1] * row_ele`), same bits.
+// approach 3 (ILU_0_gpu.cu:693-935): sum = sum of l_ik*u_kj (fma) over k in
+// ascending order starting from 0, then a_ij = (a_ij - sum)/d with d = u_jj
+// below the diagonal and d = 1 elsewhere.
+// approach 2 (ILU_0_gpu.cu:376-685): as approach 3 but the dependency list
+// is a linked list built by head insertion, so k runs DESCENDING.
+ORC_API void orc_ilu0(int n, int nnz, const int* rp, const int* ci, int nsys, const double* vals, double* lu,
+                      int approach) {
+  std::vector<int> diag(n);
+  orc_find_diag(n, rp, ci, diag.data());
+#pragma omp parallel for schedule(static)
+  for (int s = 0; s < nsys; ++s) {
+    double* a = lu + (size_t)s * nnz;
+    std::memcpy(a, vals + (size_t)s * nnz, sizeof(double) * nnz);
+    std::vector<int> colpos(n, -1);
+    std::vector<int> ks;
+    std::vector<std::pair<int, int>> pairs;  // (pos_ik, pos_kj)
+    for (int i = 0; i < n; ++i) {
+      for (int k = rp[i]; k < rp[i + 1]; ++k) colpos[ci[k]] = k;
+      for (int e = rp[i]; e < rp[i + 1]; ++e) {
+        const int j = ci[e];
+        const int kmax = std::min(i, j);  // k < min(i, j)
+        pairs.clear();
+        for (int lk = rp[i]; lk < rp[i + 1] && ci[lk] < kmax; ++lk) {
+          const int k = ci[lk];
+          for (int uk = diag[k] + 1; uk < rp[k + 1]; ++uk)
+            if (ci[uk] == j) pairs.emplace_back(lk, uk);
+        }
+        if (approach == 1 || approach == 4) {
+          double v = a[e];
+          for (auto& p : pairs) v = std::fma(-a[p.first], a[p.second], v);
+          if (j < i) v = v / a[diag[j]];
+          a[e] = v;
+        } else {
+          double sum = 0.0;
+          if (approach == 3) {
+            for (auto& p : pairs) sum = std::fma(a[p.first], a[p.second], sum);
+          } else {
+            for (auto it = pairs.rbegin(); it != pairs.rend(); ++it) sum = std::fma(a[it->first], a[it->second], sum);
+          }
+          double v = a[e] - sum;
+          if (j < i) v = v / a[diag[j]];
+          a[e] = v;
+        }
+      }
+      for (int k = rp[i]; k < rp[i + 1]; ++k) colpos[ci[k]] = -1;
+    }
+  }
+}
+
+// ParILU(0) sweep (parILU_0_gpu.cu:18-57) with the dependency list of
+// create_dependency_graph_parilu (parILU_0_gpu.cu:118-220): for entry (i,j),
+// sum = sum over k < min(i,j) ascending of l_ik*u_kj (fma from 0), then
+// (a_ij - sum)/u_jj below the diagonal and (a_ij - sum)/1 on and above it.
+// The reference updates in place without a barrier inside a sweep (its
+// result depends on thread timing when nnz > blockDim); this restatement
+// uses the documented deterministic schedule of the library: Jacobi sweeps
+// (every entry of sweep t+1 reads the values of sweep t).  Initial guess
+// (Fill_L_and_U, factorization.cu:288-344): L = strict-lower(A) + I,
+// U = upper(A), i.e. the in-place factors start equal to A; `init` overrides.
+ORC_API void orc_parilu0(int n, int nnz, const int* rp, const int* ci, int nsys, const double* vals,
+                         const double* init, int sweeps, double* lu) {
+  std::vector<int> diag(n);
+  orc_find_diag(n, rp, ci, diag.data());
+  // dependency lists (pattern only)
+  std::vector<int> dptr(nnz + 1, 0), dl, du;
+  for (int i = 0; i < n; ++i)
+    for (int e = rp[i]; e < rp[i + 1]; ++e) {
+      const int j = ci[e];
+      const int kmax = std::min(i, j);
+      for (int lk = rp[i]; lk < rp[i + 1] && ci[lk] < kmax; ++lk) {
+        const int k = ci[lk];
+        for (int uk = diag[k] + 1; uk < rp[k + 1]; ++uk)
+          if (ci[uk] == j) {
+            dl.push_back(lk);
+            du.push_back(uk);
+          }
+      }
+      dptr[e + 1] = (int)dl.size();
+    }
+  std::vector<int> rowof(nnz);
+  for (int i = 0; i < n; ++i)
+    for (int e = rp[i]; e < rp[i + 1]; ++e) rowof[e] = i;
+#pragma omp parallel for schedule(static)
+  for (int s = 0; s < nsys; ++s) {
+    const double* A = vals + (size_t)s * nnz;
+    double* cur = lu + (size_t)s * nnz;
+    std::memcpy(cur, init ? init + (size_t)s * nnz : A, sizeof(double) * nnz);
+    std::vector<double> nxt(nnz);
+    for (int t = 0; t < sweeps; ++t) {
+      for (int e = 0; e < nnz; ++e) {
+        double sum = 0.0;
+        for (int q = dptr[e]; q < dptr[e + 1]; ++q) sum = std::fma(cur[dl[q]], cur[du[q]], sum);
+        double v = A[e] - sum;
+        const int i = rowof[e], j = ci[e];
+        if (j < i) v = v / cur[diag[j]];
+        nxt[e] = v;
+      }
+      std::memcpy(cur, nxt.data(), sizeof(double) * nnz);
+    }
+  }
+}
+
+// ||(A - L U)|_S||_F / ||A||_F on the factor pattern S (the ILU residual that
+// judges a ParILU warm start; no reference counterpart).  Products summed in
+// ascending k with fma, in double.
+ORC_API void orc_ilu_residual(int n, int nnz, const int* rp, const int* ci, int nsys, const double* vals,
+                              const double* lu, double* out) {
+  std::vector<int> diag(n);
+  orc_find_diag(n, rp, ci, diag.data());
+#pragma omp parallel for schedule(static)
+  for (int s = 0; s < nsys; ++s) {
+    const double* A = vals + (size_t)s * nnz;
+    const double* F = lu + (size_t)s * nnz;
+    double num = 0.0, den = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int e = rp[i]; e < rp[i + 1]; ++e) {
+        const int j = ci[e];
+        // (LU)_ij = sum_{k <= min(i,j)} l_ik u_kj, l_ii = 1
+        double acc = 0.0;
+        for (int lk = rp[i]; lk < rp[i + 1] && ci[lk] <= std::min(i, j); ++lk) {
+          const int k = ci[lk];
+          const double l = (k == i) ? 1.0 : F[lk];
+          if (k == j && k < i) {  // u_jj with j < i
+            acc = std::fma(l, F[diag[j]], acc);
+            continue;
+          }
+          for (int uk = diag[k]; uk < rp[k + 1]; ++uk)
+            if (ci[uk] == j) acc = std::fma(l, F[uk], acc);
+        }
+        const double d = A[e] - acc;
+        num = std::fma(d, d, num);
+        den = std::fma(A[e], A[e], den);
+      }
+    out[s] = std::sqrt(num) / std::sqrt(den);
+  }
+}
+
+// ===========================================================================
+// ISAI (isai_gpu.cu)
+// ===========================================================================
+
+// Pattern of |T|^power (isai_gpu.cu:40-179).  The reference forms the powers
+// densely from page 0's numeric values, so an entry is in the pattern when
+// the computed value is nonzero; with vals0 == NULL the structural pattern is
+// returned instead (identical unless an entry cancels to exactly 0).
+// Returns nnz; ai_rp / ai_ci may be NULL for a size query.
+ORC_API int orc_isai_pattern(int n, const int* rp, const int* ci, int power, const double* vals0, int* ai_rp,
+                             int* ai_ci) {
+  // dense column-major n x n, same summation order as the reference
+  std::vector<double> cur((size_t)n * n, 0.0), nxt;
+  for (int r = 0; r < n; ++r)
+    for (int k = rp[r]; k < rp[r + 1]; ++k) cur[(size_t)ci[k] * n + r] = vals0 ? vals0[k] : 1.0;
+  std::vector<double> base = cur;
+  for (int p = 2; p <= power; ++p) {
+    nxt.assign((size_t)n * n, 0.0);
+    for (int col = 0; col < n; ++col)
+      for (int r = 0; r < n; ++r) {
+        double sum = 0.0;
+        for (int k = rp[r]; k < rp[r + 1]; ++k) {
+          const double v = vals0 ? vals0[k] : 1.0;
+          // host code, x86 without FMA contraction: separate multiply and add
+          sum = sum + v * cur[(size_t)col * n + ci[k]];
+        }
+        nxt[(size_t)col * n + r] = sum;
+      }
+    cur.swap(nxt);
+  }
+  int nz = 0;
+  if (ai_rp) ai_rp[0] = 0;
+  for (int r = 0; r < n; ++r) {
+    for (int col = 0; col < n; ++col)
+      if (cur[(size_t)col * n + r] != 0.0) {
+        if (ai_ci) ai_ci[nz] = col;
+        ++nz;
+      }
+    if (ai_rp) ai_rp[r + 1] = nz;
+  }
+  return nz;
+}
+
+// ISAI values (isai_gpu.cu:209-287 extraction, 325-389 and 559-626 solves).
+// For row i of M with pattern J (sorted, |J| <= 32): the reference loads
+// lane t with row t of T(J,J)^T and solves
+//   lower T (tri = 0): upper-triangular back substitution, rhs e_{|J|-1}
+//     (solve_upper_tri_dense): for col = |J|-1 .. 0: lane col divides by its
+//     diagonal, then lanes t < col do sol_t = fma(-sol_col, T(J_col,J_t), sol_t)
+//   upper T (tri = 1): forward substitution, rhs e_0 (solve_lower_tri_dense):
+//     for col = 0 .. |J|-1, lanes t > col update.
+// Missing entries of T(J,J) are zeros (they give exact zero updates).
+// T is given in the reference's separate CSR form (t_rp/t_ci/t_vals; for L
+// the explicit unit diagonal is part of the pattern).
+ORC_API int orc_isai_values(int n, const int* t_rp, const int* t_ci, int t_nnz, int nsys, const double* t_vals,
+                            int tri, const int* ai_rp, const int* ai_ci, int ai_nnz, double* ai_vals) {
+  for (int i = 0; i < n; ++i)
+    if (ai_rp[i + 1] - ai_rp[i] > 32) return -1;
+#pragma omp parallel for schedule(static)
+  for (int s = 0; s < nsys; ++s) {
+    const double* T = t_vals + (size_t)s * t_nnz;
+    double* M = ai_vals + (size_t)s * ai_nnz;
+    double loc[32][32];  // loc[t][c] = T(J_c, J_t)
+    for (int i = 0; i < n; ++i) {
+      const int beg = ai_rp[i], sz = ai_rp[i + 1] - ai_rp[i];
+      const int* J = ai_ci + beg;
+      for (int t = 0; t < sz; ++t)
+        for (int c = 0; c < sz; ++c) {
+          double v = 0.0;
+          for (int k = t_rp[J[c]]; k < t_rp[J[c] + 1]; ++k)
+            if (t_ci[k] == J[t]) v = T[k];
+          loc[t][c] = v;
+        }
+      double sol[32];
+      if (tri == 0) {
+        for (int t = 0; t < sz; ++t) sol[t] = (t == sz - 1) ? 1.0 : 0.0;
+        for (int col = sz - 1; col >= 0; --col) {
+          sol[col] = sol[col] / loc[col][col];
+          const double bot = sol[col];
+          for (int t = 0; t < col; ++t) sol[t] = std::fma(-bot, loc[t][col], sol[t]);
+        }
+      } else {
+        for (int t = 0; t < sz; ++t) sol[t] = (t == 0) ? 1.0 : 0.0;
+        for (int col = 0; col < sz; ++col) {
+          sol[col] = sol[col] / loc[col][col];
+          const double top = sol[col];
+          for (int t = col + 1; t < sz; ++t) sol[t] = std::fma(-top, loc[t][col], sol[t]);
+        }
+      }
+      for (int t = 0; t < sz; ++t) M[beg + t] = sol[t];
+    }
+  }
+  return 0;
+}
+
+// ===========================================================================
+// BiCGSTAB (KernelBatchedPreconditionedBiCGSTAB_ILU in
+// PrecondBiCGSTAB_exact_ilu0_app1_merged_gpu.cu:249-538 and
+// PrecondBiCGSTAB_ilu_gpu.cu:155-438; KernelBatchedPreconditionedBiCGSTAB_ILU_ISAI
+// in PrecondBiCGSTAB_ilu_isai_gpu.cu:49-262)
+// ===========================================================================
+//
+// prec: 0 = in-place LU factors (lu on the factor pattern f_rp/f_ci = A's
+//           pattern with inserted diagonals; NULL = A's), triangular solves;
+//       1 = ISAI: z = aiU * (aiL * v), both with the SpMV tree order;
+//       2 = identity;
+//       3 = in-place LU stored as float (lu_f32), applied in FP32 (library mode);
+//       4 = ISAI stored as float (ail_f/aiu_f), applied in FP32.
+// dot: 0 = warp-0 tree inner products (ILU solver kernels),
+//      1 = serial inner products (ISAI solver kernel).
+// tol_mode: 0 = absolute (||r|| < tol, the reference's ATOL), 1 = relative to ||b||.
+// Outputs per system: x, iteration count (0.5 steps), conv flag (1/-1),
+// recursive residual norm and a detailed status (BILU_SYS_* values).
+ORC_API void orc_bicgstab(int n, int nnz, const int* rp, const int* ci, int nsys, const double* A, const double* b,
+                          int f_nnz, const int* f_rp, const int* f_ci, int prec, const double* lu,
+                          const float* lu_f32, int ail_nnz, const int* ail_rp,
+                          const int* ail_ci, const double* ail, const float* ail_f, int aiu_nnz, const int* aiu_rp,
+                          const int* aiu_ci, const double* aiu, const float* aiu_f, int dot, int tol_mode,
+                          double tol, int max_iter, double* x_out, float* iters_out, int* conv_out,
+                          double* res_out, int* status_out) {
+  // factor pattern (A's pattern with inserted diagonals); defaults to A's
+  if (!f_rp) {
+    f_rp = rp;
+    f_ci = ci;
+    f_nnz = nnz;
+  }
+  std::vector<int> diag(n);
+  orc_find_diag(n, f_rp, f_ci, diag.data());
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int s = 0; s < nsys; ++s) {
+    const double* As = A + (size_t)s * nnz;
+    const double* bs = b + (size_t)s * n;
+    const double* LU = lu ? lu + (size_t)s * f_nnz : nullptr;
+    const float* LUf = lu_f32 ? lu_f32 + (size_t)s * f_nnz : nullptr;
+    const double* AIL = ail ? ail + (size_t)s * ail_nnz : nullptr;
+    const double* AIU = aiu ? aiu + (size_t)s * aiu_nnz : nullptr;
+    const float* AILf = ail_f ? ail_f + (size_t)s * ail_nnz : nullptr;
+    const float* AIUf = aiu_f ? aiu_f + (size_t)s * aiu_nnz : nullptr;
+    std::vector<double> x(n, 0.0), r(n), rh(n), p(n, 0.0), v(n, 0.0), sv(n), t(n), ph(n), sh(n), tmp(n);
+    std::vector<float> yf(n), rinvf(n), fin(n), fmid(n);
+    if (prec == 3)
+      for (int i = 0; i < n; ++i) rinvf[i] = (float)(1.0 / (double)LUf[diag[i]]);
+    auto dotf = [&](const double* a1, const double* a2) {
+      return dot == 0 ? dot_warp0(n, a1, a2) : dot_serial(n, a1, a2);
+    };
+    auto apply = [&](const double* in, double* out) {
+      if (prec == 0) {
+        trsv_lu(n, f_rp, f_ci, diag.data(), LU, in, tmp.data(), out);
+      } else if (prec == 1) {
+        spmv_tree(n, ail_rp, ail_ci, AIL, in, tmp.data());
+        spmv_tree(n, aiu_rp, aiu_ci, AIU, tmp.data(), out);
+      } else if (prec == 3) {
+        trsv_lu_f32(n, f_rp, f_ci, diag.data(), LUf, rinvf.data(), in, yf.data(), out);
+      } else if (prec == 4) {
+        for (int i = 0; i < n; ++i) fin[i] = (float)in[i];
+        spmv_f32(n, ail_rp, ail_ci, AILf, fin.data(), fmid.data());
+        spmv_f32(n, aiu_rp, aiu_ci, AIUf, fmid.data(), fin.data());
+        for (int i = 0; i < n; ++i) out[i] = (double)fin[i];
+      } else {
+        for (int i = 0; i < n; ++i) out[i] = in[i];
+      }
+    };
+    // initialization (Bicgstab_common.hpp:151-192): x = 0, r = b - A*0 = b, r_hat = r
+    for (int i = 0; i < n; ++i) r[i] = bs[i];
+    rh = r;
+    const double res_initial = std::sqrt(dotf(r.data(), r.data()));
+    const double b_norm = std::sqrt(dotf(bs, bs));
+    const double thr = (tol_mode == 0) ? tol : tol * b_norm;
+    double rho_old = 1, rho_new = 1, omega_old = 1, omega_new = 1, alpha = 1, beta = 1;
+    double res = res_initial;
+    float iter = 0;
+    int conv = -1, status = -1;
+    if (b_norm == 0) {
+      std::fill(x.begin(), x.end(), 0.0);
+      iter = 0;
+      conv = 1;
+      res = 0;
+      status = 2;
+    } else if (res_initial < thr) {
+      iter = 0;
+      conv = 1;
+      status = 3;
+    } else {
+      while (iter < (float)max_iter) {
+        rho_new = dotf(r.data(), rh.data());
+        if (rho_new == 0) {
+          status = -2;
+          break;
+        }
+        beta = (rho_new / rho_old) * (alpha / omega_old);
+        for (int i = 0; i < n; ++i) p[i] = std::fma(beta, std::fma(-omega_old, v[i], p[i]), r[i]);
+        apply(p.data(), ph.data());
+        spmv_tree(n, rp, ci, As, ph.data(), v.data());
+        const double rv = dotf(rh.data(), v.data());
+        alpha = rho_new / rv;
+        for (int i = 0; i < n; ++i) sv[i] = std::fma(-alpha, v[i], r[i]);
+        res = std::sqrt(dotf(sv.data(), sv.data()));
+        iter = iter + 0.5f;
+        if (res < thr) {
+          for (int i = 0; i < n; ++i) x[i] = std::fma(alpha, ph[i], x[i]);
+          conv = 1;
+          status = 1;
+          break;
+        }
+        apply(sv.data(), sh.data());
+        spmv_tree(n, rp, ci, As, sh.data(), t.data());
+        const double ts = dotf(t.data(), sv.data());
+        const double tt = dotf(t.data(), t.data());
+        omega_new = ts / tt;
+        for (int i = 0; i < n; ++i) x[i] = std::fma(omega_new, sh[i], std::fma(alpha, ph[i], x[i]));
+        iter = iter + 0.5f;
+        for (int i = 0; i < n; ++i) r[i] = std::fma(-omega_new, t[i], sv[i]);
+        res = std::sqrt(dotf(r.data(), r.data()));
+        rho_old = rho_new;
+        omega_old = omega_new;
+        if (res < thr) {
+          conv = 1;
+          status = 1;
+          break;
+        }
+      }
+      if (status == -1 && !(std::isfinite(res))) status = -3;
+    }
+    std::memcpy(x_out + (size_t)s * n, x.data(), sizeof(double) * n);
+    if (iters_out) iters_out[s] = iter;
+    if (conv_out) conv_out[s] = conv;
+    if (res_out) res_out[s] = res;
+    if (status_out) status_out[s] = status;
+  }
+}
+
+// KernelFillTrueResNorms (Bicgstab_common.hpp:294-342): r = b - A x with the
+// SpMV tree order, norm = sqrt of the SERIAL inner product.
+ORC_API void orc_true_residual(int n, int nnz, const int* rp, const int* ci, int nsys, const double* A,
+                               const double* b, const double* x, double* out) {
+#pragma omp parallel for schedule(static)
+  for (int s = 0; s < nsys; ++s) {
+    const double* As = A + (size_t)s * nnz;
+    const double* bs = b + (size_t)s * n;
+    const double* xs = x + (size_t)s * n;
+    std::vector<double> r(n);
+    for (int i = 0; i < n; ++i) r[i] = bs[i] - row_tree(As, ci, rp[i], rp[i + 1], xs);
+    out[s] = std::sqrt(dot_serial(n, r.data(), r.data()));
+  }
+}
+
+// ===========================================================================
+// FP64 dense LU with partial pivoting (forward-error oracle; no reference
+// counterpart).  Solves each system densely; returns x.
+// ===========================================================================
+ORC_API void orc_dense_solve(int n, int nnz, const int* rp, const int* ci, int nsys, const int* sys_ids,
+                             const double* A, const double* b, double* x_out) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int q = 0; q < nsys; ++q) {
+    const int s = sys_ids ? sys_ids[q] : q;
+    std::vector<double> M((size_t)n * n, 0.0), y(b + (size_t)s * n, b + (size_t)s * n + n);
+    const double* As = A + (size_t)s * nnz;
+    for (int i = 0; i < n; ++i)
+      for (int k = rp[i]; k < rp[i + 1]; ++k) M[(size_t)i * n + ci[k]] = As[k];
+    std::vector<int> piv(n);
+    for (int k = 0; k < n; ++k) {
+      int pr = k;
+      double best = std::fabs(M[(size_t)k * n + k]);
+      for (int i = k + 1; i < n; ++i) {
+        const double v = std::fabs(M[(size_t)i * n + k]);
+        if (v > best) {
+          best = v;
+          pr = i;
+        }
+      }
+      if (pr != k) {
+        for (int j = 0; j < n; ++j) std::swap(M[(size_t)k * n + j], M[(size_t)pr * n + j]);
+        std::swap(y[k], y[pr]);
+      }
+      const double d = M[(size_t)k * n + k];
+      for (int i = k + 1; i < n; ++i) {
+        const double f = M[(size_t)i * n + k] / d;
+        if (f == 0.0) continue;
+        M[(size_t)i * n + k] = f;
+        for (int j = k + 1; j < n; ++j) M[(size_t)i * n + j] = std::fma(-f, M[(size_t)k * n + j], M[(size_t)i * n + j]);
+        y[i] = std::fma(-f, y[k], y[i]);
+      }
+    }
+    double* xs = x_out + (size_t)q * n;
+    for (int i = n - 1; i >= 0; --i) {
+      double acc = y[i];
+      for (int j = i + 1; j < n; ++j) acc = std::fma(-M[(size_t)i * n + j], xs[j], acc);
+      xs[i] = acc / M[(size_t)i * n + i];
+    }
+  }
+}
+
+ORC_API int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+ORC_API void orc_set_num_threads(int t) {
+#ifdef _OPENMP
+  if (t > 0) omp_set_num_threads(t);
+#else
+  (void)t;
+#endif
+}

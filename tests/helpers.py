@@ -1,0 +1,98 @@
+"""Shared helpers of the test suite: seeded workloads, the oracle pipeline
+that mirrors each preconditioner family, and GPU calls through the C ABI."""
+import numpy as np
+
+import bilu
+import oracle as O
+
+SEED = 20261203
+
+# Small members of the benchmark families (kind, gx, gy, gz): every parity
+# case runs the same generator as the benchmark with a smaller grid.
+FAMILIES = {
+    "2d5_8x8": (1, 8, 8, 1),
+    "2d5_16x16": (1, 16, 16, 1),
+    "3d7_5x5x5": (2, 5, 5, 5),
+    "cd2d_12x12": (4, 12, 12, 1),
+    "3d7_7x7x7": (5, 7, 7, 7),
+}
+
+
+def workload(name, nsys, seed=SEED):
+    kind, gx, gy, gz = FAMILIES[name]
+    return bilu.gen_stencil(kind, gx, gy, gz, nsys, seed)
+
+
+def oracle_pipeline(rp, ci, vals, b, precond, approach=1, sweeps=5, fp32=False, tol_mode=0, tol=1e-11,
+                    max_iter=500, isai_power=2, lu_init=None):
+    """The reference's computation for one preconditioner family, restated on the CPU."""
+    out = {}
+    if precond == bilu.PRECOND_NONE:
+        r = O.bicgstab(rp, ci, vals, b, prec=O.PREC_NONE, dot=0, tol_mode=tol_mode, tol=tol, max_iter=max_iter)
+        r["true_res"] = O.true_residual(rp, ci, vals, b, r["x"])
+        return r
+    nrp, nci, src = O.add_missing_diag(rp, ci)
+    fvals = np.where(src[None, :] >= 0, vals[:, np.maximum(src, 0)], 0.0)
+    if precond in (bilu.PRECOND_ILU0, bilu.PRECOND_ILU0_SPLIT, bilu.PRECOND_ILU0_ISAI):
+        lu = O.ilu0(nrp, nci, fvals, approach)
+    else:
+        lu = O.parilu0(nrp, nci, fvals, sweeps, init=lu_init)
+    out["lu"] = lu
+    if precond in (bilu.PRECOND_ILU0_ISAI, bilu.PRECOND_PARILU0_ISAI):
+        lrp, lci, urp, uci = O.split_pattern(nrp, nci)
+        L, U = O.split_values(nrp, nci, lu)
+        arp, aci = O.isai_pattern(lrp, lci, isai_power)
+        brp, bci = O.isai_pattern(urp, uci, isai_power)
+        ail = O.isai_values(lrp, lci, L, 0, arp, aci)
+        aiu = O.isai_values(urp, uci, U, 1, brp, bci)
+        out.update(ail=ail, aiu=aiu, ail_pattern=(arp, aci), aiu_pattern=(brp, bci))
+        if fp32:
+            r = O.bicgstab(rp, ci, vals, b, prec=O.PREC_ISAI_F32, ail=(arp, aci, None), aiu=(brp, bci, None),
+                           ail_f32=ail.astype(np.float32), aiu_f32=aiu.astype(np.float32), dot=1,
+                           tol_mode=tol_mode, tol=tol, max_iter=max_iter)
+        else:
+            r = O.bicgstab(rp, ci, vals, b, prec=O.PREC_ISAI, ail=(arp, aci, ail), aiu=(brp, bci, aiu), dot=1,
+                           tol_mode=tol_mode, tol=tol, max_iter=max_iter)
+    else:
+        fp = (nrp, nci)
+        if fp32:
+            r = O.bicgstab(rp, ci, vals, b, prec=O.PREC_LU_F32, lu_f32=lu.astype(np.float32), dot=0,
+                           tol_mode=tol_mode, tol=tol, max_iter=max_iter, factor_pattern=fp)
+        else:
+            r = O.bicgstab(rp, ci, vals, b, prec=O.PREC_LU, lu=lu, dot=0, tol_mode=tol_mode, tol=tol,
+                           max_iter=max_iter, factor_pattern=fp)
+    out.update(r)
+    out["true_res"] = O.true_residual(rp, ci, vals, b, r["x"])
+    return out
+
+
+def gpu_solve(dev, rp, ci, vals, b, lu_init=None, **opts):
+    """Solve through the C ABI; returns numpy results and the plan info."""
+    import torch
+    nsys, n = b.shape
+    with bilu.Plan(rp, ci, **opts) as plan:
+        V = torch.from_numpy(vals).to(dev)
+        B = torch.from_numpy(b).to(dev)
+        X = torch.full_like(B, float("nan"))
+        it = torch.full((nsys,), -7.0, dtype=torch.float32, device=dev)
+        cv = torch.full((nsys,), 7, dtype=torch.int32, device=dev)
+        rs = torch.full((nsys,), -1.0, dtype=torch.float64, device=dev)
+        tr = torch.full((nsys,), -1.0, dtype=torch.float64, device=dev)
+        st = torch.full((nsys,), 99, dtype=torch.int32, device=dev)
+        LI = None if lu_init is None else torch.from_numpy(lu_init).to(dev)
+        plan.solve(V, B, X, it, cv, rs, tr, st, lu_init=LI)
+        torch.cuda.synchronize()
+        info = plan.info()
+    return {"x": X.cpu().numpy(), "iters": it.cpu().numpy(), "conv": cv.cpu().numpy(), "res": rs.cpu().numpy(),
+            "true_res": tr.cpu().numpy(), "status": st.cpu().numpy(), "info": info}
+
+
+def assert_bitwise(a, b, what):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, f"{what}: shape {a.shape} vs {b.shape}"
+    same = (a == b) | (np.isnan(a) & np.isnan(b)) if a.dtype.kind == "f" else (a == b)
+    if not np.all(same):
+        idx = np.argwhere(~same)[:5]
+        raise AssertionError(f"{what}: {int((~same).sum())} of {a.size} differ, first at {idx.tolist()}: "
+                             f"{a[tuple(idx[0])]!r} vs {b[tuple(idx[0])]!r}")

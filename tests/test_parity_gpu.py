@@ -1,0 +1,214 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the oracle.
+
+In the reference operation order (BILU_REDUCE_REF) every output is compared
+bit for bit: iteration counts, convergence flags, statuses, the solution,
+the recursive residual norm and the true residual norm, for every
+preconditioner family on small members of the benchmark workloads."""
+import numpy as np
+import pytest
+
+import bilu
+import helpers as H
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+NSYS = 24
+
+
+def _compare(g, o, what, fields=("iters", "conv", "x", "res", "true_res")):
+    for f in fields:
+        H.assert_bitwise(g[f], o[f], f"{what}: {f}")
+    np.testing.assert_array_equal(g["status"], o["status"], err_msg=f"{what}: status")
+
+
+@pytest.mark.parametrize("family", ["2d5_8x8", "2d5_16x16", "3d7_5x5x5", "cd2d_12x12", "3d7_7x7x7"])
+@pytest.mark.parametrize("approach", [1, 2, 3, 4])
+def test_merged_ilu0_bitwise(cuda, family, approach):
+    rp, ci, v, b = H.workload(family, NSYS)
+    o = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_ILU0, approach=approach)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0, ilu_approach=approach)
+    _compare(g, o, f"merged ILU(0) {family} approach {approach}")
+    assert np.all(o["conv"] == 1)
+
+
+@pytest.mark.parametrize("family", ["2d5_16x16", "3d7_5x5x5"])
+@pytest.mark.parametrize("approach", [1, 3])
+def test_split_ilu0_bitwise(cuda, family, approach):
+    rp, ci, v, b = H.workload(family, NSYS)
+    o = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_ILU0_SPLIT, approach=approach)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0_SPLIT, ilu_approach=approach)
+    _compare(g, o, f"split ILU(0) {family} approach {approach}")
+
+
+@pytest.mark.parametrize("family", ["2d5_16x16", "3d7_7x7x7"])
+@pytest.mark.parametrize("sweeps", [0, 1, 5])
+def test_parilu0_bitwise(cuda, family, sweeps):
+    rp, ci, v, b = H.workload(family, NSYS)
+    o = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_PARILU0, sweeps=sweeps)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_PARILU0, parilu_sweeps=sweeps)
+    _compare(g, o, f"ParILU(0) {family} sweeps {sweeps}")
+
+
+@pytest.mark.parametrize("family", ["2d5_16x16", "3d7_5x5x5", "3d7_7x7x7"])
+@pytest.mark.parametrize("precond", [bilu.PRECOND_ILU0_ISAI, bilu.PRECOND_PARILU0_ISAI])
+def test_isai_bitwise(cuda, family, precond):
+    rp, ci, v, b = H.workload(family, NSYS)
+    o = H.oracle_pipeline(rp, ci, v, b, precond, approach=3, sweeps=5)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, ilu_approach=3, parilu_sweeps=5)
+    _compare(g, o, f"ISAI precond {precond} {family}")
+
+
+@pytest.mark.parametrize("precond", [bilu.PRECOND_ILU0, bilu.PRECOND_PARILU0, bilu.PRECOND_PARILU0_ISAI])
+def test_fp32_factors_bitwise(cuda, precond):
+    rp, ci, v, b = H.workload("cd2d_12x12", NSYS)
+    o = H.oracle_pipeline(rp, ci, v, b, precond, fp32=True, tol_mode=1, tol=1e-10)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, factor_precision=bilu.FP32, tol_mode=1, tol=1e-10)
+    _compare(g, o, f"FP32 factors precond {precond}")
+    assert np.all(g["conv"] == 1)
+
+
+@pytest.mark.parametrize("precond", [bilu.PRECOND_NONE])
+def test_unpreconditioned_bitwise(cuda, precond):
+    rp, ci, v, b = H.workload("2d5_8x8", NSYS)
+    o = H.oracle_pipeline(rp, ci, v, b, precond)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond)
+    _compare(g, o, "no preconditioner")
+
+
+def test_relative_tolerance_bitwise(cuda):
+    rp, ci, v, b = H.workload("2d5_16x16", NSYS)
+    o = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_ILU0, tol_mode=1, tol=1e-10)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0, tol_mode=bilu.TOL_REL, tol=1e-10)
+    _compare(g, o, "relative tolerance")
+    assert np.all(g["res"] < 1e-10 * np.linalg.norm(b, axis=1))
+
+
+@pytest.mark.parametrize("precond", [bilu.PRECOND_ILU0, bilu.PRECOND_PARILU0, bilu.PRECOND_PARILU0_ISAI])
+def test_fast_mode_properties(cuda, precond):
+    """FAST order is not bit-comparable; it must converge to the same accuracy in about as many iterations."""
+    rp, ci, v, b = H.workload("3d7_7x7x7", NSYS)
+    ref = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, tol_mode=1, tol=1e-10)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, tol_mode=1, tol=1e-10, reduction=bilu.REDUCE_FAST)
+    bn = np.linalg.norm(b, axis=1)
+    assert np.all(g["conv"] == 1)
+    assert np.all(np.abs(g["iters"] - ref["iters"]) <= 1.0)
+    assert np.all(g["res"] < 1e-10 * bn)
+    # true residual within a small factor of the recursive one (rounding drift)
+    assert np.all(g["true_res"] < 1e-9 * bn)
+    xd = O.dense_solve(rp, ci, v, b)
+    assert np.max(np.abs(g["x"] - xd)) < 1e-8
+
+
+# ---------------------------------------------------------------- separate entry points
+def test_factorisation_entry_points_bitwise(cuda):
+    import torch
+    rp, ci, v, b = H.workload("3d7_5x5x5", NSYS)
+    with bilu.Plan(rp, ci, precond=bilu.PRECOND_PARILU0_ISAI) as plan:
+        V = torch.from_numpy(v).to(cuda)
+        for approach in (1, 2, 3, 4):
+            LU = torch.empty_like(V)
+            plan.ilu0(V, LU, approach)
+            H.assert_bitwise(LU.cpu().numpy(), O.ilu0(rp, ci, v, approach), f"bilu_ilu0 approach {approach}")
+        for sweeps in (1, 3, 7):
+            LU = torch.empty_like(V)
+            plan.parilu0(V, LU, sweeps)
+            H.assert_bitwise(LU.cpu().numpy(), O.parilu0(rp, ci, v, sweeps), f"bilu_parilu0 sweeps {sweeps}")
+        lu = O.ilu0(rp, ci, v, 3)
+        LU = torch.from_numpy(lu).to(cuda)
+        Lr, Ur = O.split_values(rp, ci, lu)
+        Lg = torch.empty((NSYS, Lr.shape[1]), dtype=torch.float64, device=cuda)
+        Ug = torch.empty((NSYS, Ur.shape[1]), dtype=torch.float64, device=cuda)
+        plan.split_lu(LU, Lg, Ug)
+        H.assert_bitwise(Lg.cpu().numpy(), Lr, "bilu_split_lu L")
+        H.assert_bitwise(Ug.cpu().numpy(), Ur, "bilu_split_lu U")
+        lrp, lci, urp, uci = O.split_pattern(rp, ci)
+        arp, aci = O.isai_pattern(lrp, lci, 2)
+        brp, bci = O.isai_pattern(urp, uci, 2)
+        grp, gci = plan.pattern(1)
+        np.testing.assert_array_equal(grp, arp)
+        np.testing.assert_array_equal(gci, aci)
+        grp, gci = plan.pattern(2)
+        np.testing.assert_array_equal(grp, brp)
+        np.testing.assert_array_equal(gci, bci)
+        AIL = torch.empty((NSYS, len(aci)), dtype=torch.float64, device=cuda)
+        AIU = torch.empty((NSYS, len(bci)), dtype=torch.float64, device=cuda)
+        plan.isai(LU, AIL, AIU)
+        H.assert_bitwise(AIL.cpu().numpy(), O.isai_values(lrp, lci, Lr, 0, arp, aci), "bilu_isai aiL")
+        H.assert_bitwise(AIU.cpu().numpy(), O.isai_values(urp, uci, Ur, 1, brp, bci), "bilu_isai aiU")
+        X = torch.from_numpy(np.random.default_rng(1).standard_normal(b.shape)).to(cuda)
+        B = torch.from_numpy(b).to(cuda)
+        out = torch.empty(NSYS, dtype=torch.float64, device=cuda)
+        plan.true_residual(V, B, X, out)
+        H.assert_bitwise(out.cpu().numpy(), O.true_residual(rp, ci, v, b, X.cpu().numpy()), "bilu_true_residual")
+
+
+# ---------------------------------------------------------------- edge cases
+def test_zero_and_tiny_rhs(cuda):
+    rp, ci, v, b = H.workload("2d5_8x8", 6)
+    b[1] = 0.0           # x = 0 without iterating (reference: "RHS ... is 0")
+    b[3] *= 1e-14        # initial residual already below ATOL
+    o = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_ILU0)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0)
+    _compare(g, o, "zero / tiny rhs")
+    assert g["status"][1] == bilu.SYS_ZERO_RHS and g["iters"][1] == 0 and np.all(g["x"][1] == 0)
+    assert g["status"][3] == bilu.SYS_INITIAL_OK and g["iters"][3] == 0
+
+
+@pytest.mark.parametrize("max_iter", [0, 1, 3])
+def test_iteration_cap(cuda, max_iter):
+    rp, ci, v, b = H.workload("3d7_5x5x5", 8)
+    o = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_NONE, max_iter=max_iter)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_NONE, max_iter=max_iter)
+    _compare(g, o, f"max_iter {max_iter}")
+    assert np.all(g["conv"] == -1) and np.all(g["status"] == bilu.SYS_MAX_ITER)
+    assert np.all(g["iters"] == max_iter)
+
+
+def test_missing_diagonal_split_path(cuda):
+    rp, ci, v, b = H.workload("2d5_8x8", NSYS)
+    # drop the diagonal of rows 5 and 40 from the pattern (values follow), make rows still solvable
+    keep = np.ones(len(ci), bool)
+    for row in (5, 40):
+        k = rp[row] + int(np.where(ci[rp[row]:rp[row + 1]] == row)[0][0])
+        keep[k] = False
+    nrp = np.concatenate([[0], np.cumsum([keep[rp[i]:rp[i + 1]].sum() for i in range(len(rp) - 1)])]).astype(np.int32)
+    nci = ci[keep]
+    nv = np.ascontiguousarray(v[:, keep])
+    # exact ILU(0) gives the inserted zero diagonals nonzero pivots through the updates of earlier rows
+    g = H.gpu_solve(cuda, nrp, nci, nv, b, precond=bilu.PRECOND_ILU0_SPLIT, max_iter=20)
+    o = H.oracle_pipeline(nrp, nci, nv, b, bilu.PRECOND_ILU0_SPLIT, max_iter=20)
+    _compare(g, o, "missing diagonals (split ILU path)")
+    assert g["info"]["missing_diag"] == 2
+    with pytest.raises(bilu.BiluError) as e:
+        bilu.Plan(nrp, nci, precond=bilu.PRECOND_ILU0)
+    assert e.value.code == bilu.ERR_PATTERN
+
+
+def test_isai_row_limit(cuda):
+    # dense lower band: |L|^2 rows exceed the 32-entry limit of the ISAI row solve
+    n = 48
+    rows = [list(range(max(0, i - 20), min(n, i + 2))) for i in range(n)]
+    rp = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int32)
+    ci = np.concatenate(rows).astype(np.int32)
+    with pytest.raises(bilu.BiluError) as e:
+        bilu.Plan(rp, ci, precond=bilu.PRECOND_ILU0_ISAI)
+    assert e.value.code == bilu.ERR_CAPACITY
+
+
+def test_empty_batch(cuda):
+    import torch
+    rp, ci, v, b = H.workload("2d5_8x8", 1)
+    with bilu.Plan(rp, ci) as plan:
+        z = torch.empty((0, len(ci)), dtype=torch.float64, device=cuda)
+        zb = torch.empty((0, 64), dtype=torch.float64, device=cuda)
+        plan.solve(z, zb, zb.clone())
+        torch.cuda.synchronize()
+
+
+def test_nonfinite_status(cuda):
+    rp, ci, v, b = H.workload("2d5_8x8", 4)
+    v[2, :] = np.nan
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0, max_iter=5)
+    assert g["conv"][2] == -1 and g["status"][2] == bilu.SYS_NONFINITE
+    assert np.all(g["conv"][[0, 1, 3]] == 1)
