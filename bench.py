@@ -249,7 +249,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="headline only, no secondary workloads")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="headline solve only: no e2e pass, secondary workloads or CPU baseline (profiling runs)")
+    ap.add_argument("--nsys", type=int, default=0, help="override the headline batch size (profiling runs)")
     args = ap.parse_args()
+    if args.nsys > 0:
+        HEADLINE["nsys"] = args.nsys
+        HEADLINE["desc"] = HEADLINE["desc"].replace("4096 FP64", f"{args.nsys} FP64")
     if args.impl == "reference":
         run_reference_arm(args)
         return
@@ -273,8 +279,13 @@ def main():
         torch.cuda.synchronize()
 
     sampler = ClockSampler(local)
-    res = measure(HEADLINE, args.steps, max(args.warmup, 3), dev, stream, sampler=sampler, e2e=True,
-                  timed_hook=barrier)
+    res = measure(HEADLINE, args.steps, max(args.warmup, 3), dev, stream, sampler=sampler,
+                  e2e=not args.kernel_only, timed_hook=barrier)
+    if args.kernel_only:
+        if rank == 0:
+            print(json.dumps({k: res[k] for k in ("name", "nsys", "ms_total", "steps", "systems_per_s", "setup_ms",
+                                                  "solve_ms", "mean_iters", "converged", "max_rel_true_res")}))
+        return
     ms = res["ms_total"]
     if dist:
         t = torch.tensor([ms], device=dev)
@@ -306,7 +317,8 @@ def main():
     flops = fp64_flops_per_iter(n, nnz, prec_nnz, HEADLINE["opts"]["precond"]) * res["mean_iters"] * nsys
     fp64_peak = 1205.0  # GFLOP/s: 602.5 G DFMA/s measured on this machine's GB300 (full-warp DFMA stream)
     cores = os.cpu_count()
-    rate, dt, used, _ = cpu_port_rate(HEADLINE, 32)
+    cpu_sample = 512
+    rate, dt, used, _ = cpu_port_rate(HEADLINE, cpu_sample)
     line = {
         "metric": METRIC, "value": value, "unit": "systems/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -329,7 +341,7 @@ def main():
         "solve_quality": {"mean_iters": res["mean_iters"], "max_iters": res["max_iters"],
                           "converged": res["converged"], "max_rel_true_residual": res["max_rel_true_res"]},
         "cpu_baseline": {"value": rate, "unit": "systems/s", "cores": used, "kind": "port",
-                         "sample": f"32 systems of the headline workload through the CPU restatement "
+                         "sample": f"{cpu_sample} systems of the headline workload through the CPU restatement "
                                    f"({dt:.2f} s, {used} OpenMP threads of {cores} host cores)"},
         "secondary": secondary,
     }
