@@ -182,6 +182,22 @@ typedef struct bilu_timing {
 bilu_status bilu_plan_enable_timing(bilu_plan* plan, int enable);
 bilu_status bilu_plan_last_timing(bilu_plan* plan, bilu_timing* timing);
 
+/* bilu_solve without any device allocation.  No counterpart in the reference
+ * (its solvers cudaMalloc and cudaFree their temporaries on every call).
+ * For callers that cannot let a solve allocate: a simulation calling the
+ * batched solver inside its time-step loop keeps a fixed device-memory
+ * footprint set at start-up, and cudaMalloc / cudaFree would also
+ * synchronise the device mid-step.  Same kernels and bit-identical results as
+ * bilu_solve; the intermediate factors live in one fixed 32 MiB device array
+ * per GPU, reserved when the library is loaded and held until exit.  Calls
+ * needing more scratch than that are rejected with BILU_ERR_CAPACITY (split
+ * the batch).  All calls on a device share the array: calls whose kernels
+ * overlap on the GPU race.  The first call on a device looks up the array's
+ * device address; make it before any stream capture.  The plan must exist
+ * already (bilu_plan_create allocates once). */
+bilu_status bilu_solve_noalloc(bilu_plan* plan, int nsys, const double* d_values, const double* d_b,
+                               double* d_x, const bilu_results* results, void* stream);
+
 /* ---------------------------------------------------------------- factorisations */
 /* ILU(0) of every system, in place layout: d_lu (nsys*nnz, factor pattern)
  * holds L (strictly lower, unit diagonal implicit) and U (upper).

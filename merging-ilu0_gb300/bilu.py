@@ -30,7 +30,7 @@ EXPORTED = [
     "bilu_plan_get_pattern", "bilu_expand_values", "bilu_solve", "bilu_solve_warm", "bilu_ilu0",
     "bilu_parilu0", "bilu_split_lu", "bilu_isai", "bilu_true_residual", "bilu_last_error",
     "bilu_version", "bilu_device_count", "bilu_gen_stencil", "bilu_gen_uneven", "bilu_plan_enable_timing",
-    "bilu_plan_last_timing",
+    "bilu_plan_last_timing", "bilu_solve_noalloc",
 ]
 
 
@@ -90,6 +90,7 @@ def lib():
         L.bilu_split_lu.argtypes = [vp, i, vp, vp, vp, vp]
         L.bilu_isai.argtypes = [vp, i, vp, vp, vp, vp]
         L.bilu_true_residual.argtypes = [vp, i, vp, vp, vp, vp, vp]
+        L.bilu_solve_noalloc.argtypes = [vp, i, vp, vp, vp, C.POINTER(Results), vp]
         L.bilu_plan_enable_timing.argtypes = [vp, i]
         L.bilu_plan_last_timing.argtypes = [vp, C.POINTER(Timing)]
         L.bilu_gen_uneven.argtypes = [i, C.c_uint64, i, i, i, i, ip, ip, ip, ip, C.POINTER(d), C.POINTER(d)]
@@ -210,6 +211,15 @@ class Plan:
         else:
             _check(lib().bilu_solve_warm(self.h, nsys, _dev(values), _dev(lu_init), _dev(b), _dev(x), C.byref(R),
                                          _stream(stream)))
+
+    def solve_noalloc(self, values, b, x, iters=None, conv=None, res=None, true_res=None, status=None,
+                      stream=None):
+        """bilu_solve_noalloc: same results as solve(), scratch in the library's fixed device array."""
+        nsys = b.shape[0] if b.dim() > 1 else b.numel() // self.n
+        R = Results(*(C.c_void_p(t.data_ptr()) if t is not None else None
+                      for t in (iters, conv, res, true_res, status)))
+        _check(lib().bilu_solve_noalloc(self.h, nsys, _dev(values), _dev(b), _dev(x), C.byref(R),
+                                        _stream(stream)))
 
     def enable_timing(self, enable=True):
         _check(lib().bilu_plan_enable_timing(self.h, 1 if enable else 0))

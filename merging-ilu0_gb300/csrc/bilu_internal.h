@@ -118,3 +118,31 @@ cudaError_t launch_true_residual(const DevPattern& p, int nsys, const double* A,
                                  double* out, int threads, cudaStream_t st);
 
 }  // namespace bilu
+
+// Plan object behind the opaque bilu_plan handle of the C ABI.
+struct bilu_plan {
+  bilu_options opts;
+  int device = 0;
+  int n = 0, nnz_in = 0, nnz = 0, missing = 0;
+  std::vector<int> in_rp, in_ci;      // caller's pattern
+  std::vector<int> rp, ci, diag, row_of, src;
+  std::vector<int> lev_lo_ptr, lev_lo_rows, lev_up_ptr, lev_up_rows;
+  int maxw_lo = 0, maxw_up = 0, maxl = 0, a_maxl = 0;
+  std::vector<int> dep_ptr;
+  std::vector<int> dep;  // pairs
+  std::vector<int> l_rp, l_ci, l_src, u_rp, u_ci, u_src;
+  bool has_isai = false;
+  std::vector<int> ail_rp, ail_ci, aiu_rp, aiu_ci;
+  std::vector<int> ail_prog_ptr, ail_prog, aiu_prog_ptr, aiu_prog;  // prog in int units (pairs)
+  int* dbuf = nullptr;
+  bilu::DevPattern dp;
+  // solver kernel configuration
+  int threads = 0;
+  bilu::SmemLayout lay;
+  // workspace
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  // stage timing events (PST / IST / OET)
+  bool timing = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+};
