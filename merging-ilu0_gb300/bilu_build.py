@@ -50,7 +50,7 @@ def _compile(src, force):
     if not force and os.path.exists(obj):
         if os.path.getmtime(obj) >= max(os.path.getmtime(path), _headers_mtime()):
             return obj, None
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp,-O3",
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp,-O3,-ffp-contract=off",
            "-I", INCLUDE, "-I", CSRC, "-c", path, "-o", obj]
     if src.endswith(".cpp"):
         cmd[1:1] = ["-x", "cu"]
