@@ -233,6 +233,37 @@ bilu_status bilu_true_residual(const bilu_plan* plan, int nsys, const double* d_
                                const double* d_b, const double* d_x, double* d_norms,
                                void* stream);
 
+/* ---------------------------------------------------------------- uneven batches */
+/* Systems of different sizes and sparsity patterns in one solve (no reference
+ * counterpart: the reference requires one pattern per batch,
+ * ReadWriteData.cpp:398-433).  Supported preconditioners: BILU_PRECOND_ILU0
+ * (merged, the reference's PrecondBiCGSTAB_exact_ilu0_app1_merged_gpu.cu
+ * arithmetic per system) and BILU_PRECOND_NONE.
+ * Host layout: systems back to back; row pointers n_s + 1 per system (local,
+ * starting at 0), columns nnz_s per system; device values / b / x are the
+ * concatenation of the systems' arrays in the same order (value offset of
+ * system s = sum of the earlier sys_nnz, vector offset = sum of the earlier sys_n).
+ * The plan sorts the systems into size buckets (n <= 128, 256, 512, 1024,
+ * larger); each bucket runs as one persistent kernel over a work queue
+ * (largest systems first), and a solve replays one CUDA graph holding every
+ * bucket launch on concurrent branches.  The graph is captured on the first
+ * solve and again whenever the device pointers change. */
+typedef struct bilu_uneven_plan bilu_uneven_plan;
+bilu_status bilu_uneven_plan_create(bilu_uneven_plan** plan, int nsys, const int* h_sys_n, const int* h_sys_nnz,
+                                    const int* h_row_ptrs, const int* h_col_idxs, const bilu_options* opts);
+bilu_status bilu_uneven_plan_destroy(bilu_uneven_plan* plan);
+/* Times every candidate CTA size (64..1024 threads, persistent grid from the
+ * occupancy of each) per bucket on the given batch and keeps the fastest.
+ * Synchronises the stream; overwrites d_x. */
+bilu_status bilu_uneven_autotune(bilu_uneven_plan* plan, const double* d_values, const double* d_b, double* d_x,
+                                 void* stream);
+bilu_status bilu_uneven_solve(bilu_uneven_plan* plan, const double* d_values, const double* d_b, double* d_x,
+                              const bilu_results* results, void* stream);
+/* Bucket `bucket` (0..4): n range (n_lo, n_hi], systems, chosen CTA size,
+ * persistent grid, shared memory per CTA, autotuned time (ms, -1 if not tuned). */
+bilu_status bilu_uneven_get_info(const bilu_uneven_plan* plan, int bucket, int* n_lo, int* n_hi, int* systems,
+                                 int* threads, int* grid, int* smem_bytes, float* tuned_ms);
+
 /* ---------------------------------------------------------------- misc */
 const char* bilu_last_error(void);
 const char* bilu_version(void);

@@ -30,7 +30,8 @@ EXPORTED = [
     "bilu_plan_get_pattern", "bilu_expand_values", "bilu_solve", "bilu_solve_warm", "bilu_ilu0",
     "bilu_parilu0", "bilu_split_lu", "bilu_isai", "bilu_true_residual", "bilu_last_error",
     "bilu_version", "bilu_device_count", "bilu_gen_stencil", "bilu_gen_uneven", "bilu_plan_enable_timing",
-    "bilu_plan_last_timing", "bilu_solve_noalloc",
+    "bilu_plan_last_timing", "bilu_solve_noalloc", "bilu_uneven_plan_create", "bilu_uneven_plan_destroy",
+    "bilu_uneven_autotune", "bilu_uneven_solve", "bilu_uneven_get_info",
 ]
 
 
@@ -91,6 +92,11 @@ def lib():
         L.bilu_isai.argtypes = [vp, i, vp, vp, vp, vp]
         L.bilu_true_residual.argtypes = [vp, i, vp, vp, vp, vp, vp]
         L.bilu_solve_noalloc.argtypes = [vp, i, vp, vp, vp, C.POINTER(Results), vp]
+        L.bilu_uneven_plan_create.argtypes = [C.POINTER(vp), i, ip, ip, ip, ip, C.POINTER(Options)]
+        L.bilu_uneven_plan_destroy.argtypes = [vp]
+        L.bilu_uneven_autotune.argtypes = [vp, vp, vp, vp, vp]
+        L.bilu_uneven_solve.argtypes = [vp, vp, vp, vp, C.POINTER(Results), vp]
+        L.bilu_uneven_get_info.argtypes = [vp, i, ip, ip, ip, ip, ip, ip, C.POINTER(C.c_float)]
         L.bilu_plan_enable_timing.argtypes = [vp, i]
         L.bilu_plan_last_timing.argtypes = [vp, C.POINTER(Timing)]
         L.bilu_gen_uneven.argtypes = [i, C.c_uint64, i, i, i, i, ip, ip, ip, ip, C.POINTER(d), C.POINTER(d)]
@@ -152,6 +158,71 @@ def gen_stencil(kind, gx, gy, gz, nsys, seed=20261203):
     _check(lib().bilu_gen_stencil(kind, gx, gy, gz, nsys, seed, C.byref(n), C.byref(nnz), _iptr(rp), _iptr(ci),
                                   _dptr(vals), _dptr(b)))
     return rp, ci, vals, b
+
+
+def gen_uneven(nsys, seed=20261203, nmin=64, nmax=1024, kmin=5, kmax=12):
+    """Seeded uneven batch: returns (sys_n, sys_nnz, row_ptrs, col_idxs, values, b), systems back to back."""
+    sn = np.zeros(nsys, np.int32)
+    sz = np.zeros(nsys, np.int32)
+    _check(lib().bilu_gen_uneven(nsys, seed, nmin, nmax, kmin, kmax, _iptr(sn), _iptr(sz), None, None, None, None))
+    rp = np.zeros(int(sn.sum()) + nsys, np.int32)
+    ci = np.zeros(int(sz.sum()), np.int32)
+    v = np.zeros(int(sz.sum()))
+    b = np.zeros(int(sn.sum()))
+    _check(lib().bilu_gen_uneven(nsys, seed, nmin, nmax, kmin, kmax, _iptr(sn), _iptr(sz), _iptr(rp), _iptr(ci),
+                                 _dptr(v), _dptr(b)))
+    return sn, sz, rp, ci, v, b
+
+
+class UnevenPlan:
+    """bilu_uneven_plan: systems with their own sizes and patterns in one graph-launched solve."""
+
+    def __init__(self, sys_n, sys_nnz, row_ptrs, col_idxs, options=None, **kw):
+        self.sys_n = np.ascontiguousarray(sys_n, np.int32)
+        self.sys_nnz = np.ascontiguousarray(sys_nnz, np.int32)
+        self.row_ptrs = np.ascontiguousarray(row_ptrs, np.int32)
+        self.col_idxs = np.ascontiguousarray(col_idxs, np.int32)
+        self.options = options if options is not None else default_options(**kw)
+        self.nsys = len(self.sys_n)
+        h = C.c_void_p()
+        _check(lib().bilu_uneven_plan_create(C.byref(h), self.nsys, _iptr(self.sys_n), _iptr(self.sys_nnz),
+                                             _iptr(self.row_ptrs), _iptr(self.col_idxs), C.byref(self.options)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().bilu_uneven_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def autotune(self, values, b, x, stream=None):
+        _check(lib().bilu_uneven_autotune(self.h, _dev(values), _dev(b), _dev(x), _stream(stream)))
+
+    def solve(self, values, b, x, iters=None, conv=None, res=None, true_res=None, status=None, stream=None):
+        R = Results(*(C.c_void_p(t.data_ptr()) if t is not None else None
+                      for t in (iters, conv, res, true_res, status)))
+        _check(lib().bilu_uneven_solve(self.h, _dev(values), _dev(b), _dev(x), C.byref(R), _stream(stream)))
+
+    def info(self):
+        out = []
+        for k in range(5):
+            v = [C.c_int() for _ in range(6)]
+            t = C.c_float()
+            _check(lib().bilu_uneven_get_info(self.h, k, *[C.byref(q) for q in v], C.byref(t)))
+            out.append(dict(n_lo=v[0].value, n_hi=v[1].value, systems=v[2].value, threads=v[3].value,
+                            grid=v[4].value, smem_bytes=v[5].value, tuned_ms=t.value))
+        return out
 
 
 # ---------------------------------------------------------------- plans

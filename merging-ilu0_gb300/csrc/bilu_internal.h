@@ -15,6 +15,14 @@ namespace bilu {
 // Records the message for bilu_last_error() and returns the code.
 bilu_status set_error(bilu_status code, const std::string& msg);
 
+// pattern analysis shared by the plans (bilu_plan.cu)
+void pattern_levels(int n, const int* rp, const int* ci, const int* diag, std::vector<int>& lo_ptr,
+                    std::vector<int>& lo_rows, int& maxw_lo, std::vector<int>& up_ptr, std::vector<int>& up_rows,
+                    int& maxw_up);
+void pattern_deps(int n, const int* rp, const int* ci, const int* diag, std::vector<int>& dep_ptr,
+                  std::vector<int>& dep);
+size_t solve_max_smem();
+
 // Device views of one pattern plan (all pointers into one device allocation).
 struct DevPattern {
   int n = 0, nnz = 0;
@@ -102,7 +110,65 @@ struct SolveArgs {
   int dot_serial = 0;  // 1: serial inner products (ISAI solver family, reference order)
 };
 
+// Shared-memory carve-up for one system; the same on host (plan creation)
+// and device (persistent kernel, per system).  Mandatory: scalars, 7 FP64
+// vectors (x, r/s, r_hat, p, v, t, p_hat/s_hat), FP32 preconditioner
+// scratch, ISAI intermediate, diagonal reciprocals; then, most re-used
+// first, factors or ISAI values and A while they fit in `budget`.
+__host__ __device__ inline SmemLayout layout_for(int n, int annz, int fnnz, int pk, bool fp32, bool fast,
+                                                 int ail_nnz, int aiu_nnz, int budget) {
+  SmemLayout L;
+  int off = 0;
+  const int fts = fp32 ? 4 : 8;
+  const bool lu = (pk == PK_ILU_INKERNEL || pk == PK_LU_GLOBAL);
+#define BILU_TAKE(dst, bytes) \
+  do {                        \
+    (dst) = off;              \
+    off = (off + (bytes) + 15) & ~15; \
+  } while (0)
+  BILU_TAKE(L.red, 128);
+  int vecd = 7 * n;
+  if (pk == PK_ILU_INKERNEL && fp32 && fnnz > vecd) vecd = fnnz;  // FP64 factorisation scratch
+  BILU_TAKE(L.vec, vecd * 8);
+  if (fp32) BILU_TAKE(L.fvec, 2 * n * 4);
+  if (pk == PK_ISAI && !fp32) BILU_TAKE(L.tmpv, n * 8);
+  if (lu && (fp32 || fast)) BILU_TAKE(L.rinv, n * fts);
+  if (lu) {
+    if (pk == PK_ILU_INKERNEL || off + fnnz * fts <= budget) BILU_TAKE(L.F, fnnz * fts);
+  } else if (pk == PK_ISAI) {
+    if (off + ail_nnz * fts <= budget) BILU_TAKE(L.ail, ail_nnz * fts);
+    if (off + aiu_nnz * fts <= budget) BILU_TAKE(L.aiu, aiu_nnz * fts);
+  }
+  if (off + annz * 8 <= budget) BILU_TAKE(L.A, annz * 8);
+#undef BILU_TAKE
+  L.total = off;
+  return L;
+}
+
+// One system of an uneven batch (own size and pattern); offsets in ints into
+// the plan's metadata buffer, value / vector offsets into the concatenated
+// batch arrays.
+struct SysDesc {
+  int n, nnz, maxw, maxl;
+  int nlev_lo, nlev_up;
+  long long val_off, vec_off;
+  int o_rp, o_ci, o_diag, o_llp, o_llr, o_lup, o_lur, o_dp, o_dep;
+};
+
+struct UnevenArgs {
+  SolveArgs base;            // tolerance, options, concatenated A / b / x, result arrays
+  const SysDesc* desc = nullptr;
+  const int* meta = nullptr;
+  const int* order = nullptr;  // systems of this bucket, longest first
+  int count = 0;
+  int* counter = nullptr;      // work-queue head (zeroed before each launch)
+  int smem_budget = 0;         // dynamic shared memory of the launch
+};
+
 // kernel launch wrappers (k_solve.cu / k_factor.cu)
+void* uneven_kernel(int fp32, int reduce_fast, int maxl);
+cudaError_t launch_uneven(const UnevenArgs& u, int threads, int grid, int fp32, int reduce_fast, int maxl,
+                          cudaStream_t st);
 cudaError_t launch_solve(const SolveArgs& a, int threads, int fp32, int reduce_fast, int maxl, cudaStream_t st);
 size_t solve_max_smem();
 cudaError_t launch_expand(const DevPattern& p, int nsys, const double* vin, double* vout, cudaStream_t st);

@@ -33,6 +33,68 @@ bilu_status set_error(bilu_status code, const std::string& msg) {
   return code;
 }
 
+// Level schedules: a row of the unit-lower solve depends on its strictly-lower
+// columns, a row of the upper solve on its strictly-upper columns; rows of one
+// level are independent.  Rows within a level ascend.
+void pattern_levels(int n, const int* rp, const int* ci, const int* diag, std::vector<int>& lo_ptr,
+                    std::vector<int>& lo_rows, int& maxw_lo, std::vector<int>& up_ptr, std::vector<int>& up_rows,
+                    int& maxw_up) {
+  auto bucket = [&](const std::vector<int>& lv, int nlev, std::vector<int>& ptr, std::vector<int>& rows, int& maxw) {
+    ptr.assign(nlev + 1, 0);
+    for (int i = 0; i < n; ++i) ptr[lv[i] + 1]++;
+    for (int l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
+    rows.assign(n, 0);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (int i = 0; i < n; ++i) rows[fill[lv[i]]++] = i;
+    maxw = 0;
+    for (int l = 0; l < nlev; ++l) maxw = std::max(maxw, ptr[l + 1] - ptr[l]);
+  };
+  std::vector<int> lev(n, 0);
+  int nl = 0;
+  for (int i = 0; i < n; ++i) {
+    int l = 0;
+    for (int k = rp[i]; k < diag[i]; ++k) l = std::max(l, lev[ci[k]] + 1);
+    lev[i] = l;
+    nl = std::max(nl, l + 1);
+  }
+  bucket(lev, nl, lo_ptr, lo_rows, maxw_lo);
+  std::vector<int> levu(n, 0);
+  int nu = 0;
+  for (int i = n - 1; i >= 0; --i) {
+    int l = 0;
+    for (int k = diag[i] + 1; k < rp[i + 1]; ++k) l = std::max(l, levu[ci[k]] + 1);
+    levu[i] = l;
+    nu = std::max(nu, l + 1);
+  }
+  bucket(levu, nu, up_ptr, up_rows, maxw_up);
+}
+
+// (l_ik, u_kj) position pairs per entry (i,j), k ascending, k < min(i, j)
+// (the dependency lists of create_dependency_graph_parilu, parILU_0_gpu.cu:118-220,
+// and of ILU approach 3, ILU_0_gpu.cu:693-756, without the written position).
+void pattern_deps(int n, const int* rp, const int* ci, const int* diag, std::vector<int>& dep_ptr,
+                  std::vector<int>& dep) {
+  (void)diag;
+  dep_ptr.assign(rp[n] + 1, 0);
+  dep.clear();
+  for (int i = 0; i < n; ++i)
+    for (int e = rp[i]; e < rp[i + 1]; ++e) {
+      const int j = ci[e];
+      const int kmax = std::min(i, j);
+      for (int lk = rp[i]; lk < rp[i + 1] && ci[lk] < kmax; ++lk) {
+        const int k = ci[lk];
+        const int* b = ci + rp[k];
+        const int* en = ci + rp[k + 1];
+        const int* it = std::lower_bound(b, en, j);
+        if (it != en && *it == j) {
+          dep.push_back(lk);
+          dep.push_back((int)(it - ci));
+        }
+      }
+      dep_ptr[e + 1] = (int)(dep.size() / 2);
+    }
+}
+
 }  // namespace bilu
 
 using namespace bilu;
@@ -58,59 +120,12 @@ int find_pos(const std::vector<int>& rp, const std::vector<int>& ci, int r, int 
   return -1;
 }
 
-// levels: lower solve (row depends on its strictly-lower columns) and upper
-// solve (row depends on its strictly-upper columns)
 void build_levels(bilu_plan& P) {
-  const int n = P.n;
-  std::vector<int> lev(n, 0);
-  int nl = 0;
-  for (int i = 0; i < n; ++i) {
-    int l = 0;
-    for (int k = P.rp[i]; k < P.diag[i]; ++k) l = std::max(l, lev[P.ci[k]] + 1);
-    lev[i] = l;
-    nl = std::max(nl, l + 1);
-  }
-  auto bucket = [&](const std::vector<int>& lv, int nlev, std::vector<int>& ptr, std::vector<int>& rows, int& maxw) {
-    ptr.assign(nlev + 1, 0);
-    for (int i = 0; i < n; ++i) ptr[lv[i] + 1]++;
-    for (int l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
-    rows.assign(n, 0);
-    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
-    for (int i = 0; i < n; ++i) rows[fill[lv[i]]++] = i;
-    maxw = 0;
-    for (int l = 0; l < nlev; ++l) maxw = std::max(maxw, ptr[l + 1] - ptr[l]);
-  };
-  bucket(lev, nl, P.lev_lo_ptr, P.lev_lo_rows, P.maxw_lo);
-  std::vector<int> levu(n, 0);
-  int nu = 0;
-  for (int i = n - 1; i >= 0; --i) {
-    int l = 0;
-    for (int k = P.diag[i] + 1; k < P.rp[i + 1]; ++k) l = std::max(l, levu[P.ci[k]] + 1);
-    levu[i] = l;
-    nu = std::max(nu, l + 1);
-  }
-  bucket(levu, nu, P.lev_up_ptr, P.lev_up_rows, P.maxw_up);
+  bilu::pattern_levels(P.n, P.rp.data(), P.ci.data(), P.diag.data(), P.lev_lo_ptr, P.lev_lo_rows, P.maxw_lo,
+                       P.lev_up_ptr, P.lev_up_rows, P.maxw_up);
 }
 
-// (l_ik, u_kj) pairs per entry, k ascending, k < min(i, j)
-void build_deps(bilu_plan& P) {
-  P.dep_ptr.assign(P.nnz + 1, 0);
-  P.dep.clear();
-  for (int i = 0; i < P.n; ++i)
-    for (int e = P.rp[i]; e < P.rp[i + 1]; ++e) {
-      const int j = P.ci[e];
-      const int kmax = std::min(i, j);
-      for (int lk = P.rp[i]; lk < P.rp[i + 1] && P.ci[lk] < kmax; ++lk) {
-        const int k = P.ci[lk];
-        const int uk = find_pos(P.rp, P.ci, k, j);
-        if (uk >= 0) {
-          P.dep.push_back(lk);
-          P.dep.push_back(uk);
-        }
-      }
-      P.dep_ptr[e + 1] = (int)(P.dep.size() / 2);
-    }
-}
+void build_deps(bilu_plan& P) { bilu::pattern_deps(P.n, P.rp.data(), P.ci.data(), P.diag.data(), P.dep_ptr, P.dep); }
 
 // structural pattern of T^power, T given by (trp, tci)
 void pattern_power(int n, const std::vector<int>& trp, const std::vector<int>& tci, int power, std::vector<int>& orp,
@@ -205,39 +220,22 @@ bilu_status build_isai(bilu_plan& P) {
 }
 
 // Shared-memory layout of the solver kernel and its CTA size.
+int prec_kind(int precond) {
+  switch (precond) {
+    case BILU_PRECOND_ILU0: return PK_ILU_INKERNEL;
+    case BILU_PRECOND_ILU0_SPLIT:
+    case BILU_PRECOND_PARILU0: return PK_LU_GLOBAL;
+    case BILU_PRECOND_ILU0_ISAI:
+    case BILU_PRECOND_PARILU0_ISAI: return PK_ISAI;
+    default: return PK_NONE;
+  }
+}
+
 void choose_layout(bilu_plan& P) {
   const bilu_options& o = P.opts;
   const int n = P.n;
-  const bool fp32 = is_fp32(o);
-  const bool fast = o.reduction == BILU_REDUCE_FAST;
-  const int fts = fp32 ? 4 : 8;
-  const int prec = o.precond;
-  const bool lu_prec = !(is_isai(prec) || prec == BILU_PRECOND_NONE);
-  int off = 0;
-  auto take = [&](int bytes) {
-    const int o2 = off;
-    off = round_up(off + bytes, 16);
-    return o2;
-  };
-  SmemLayout L;
-  L.red = take(128);
-  int vec_doubles = 7 * n;
-  if (prec == BILU_PRECOND_ILU0 && fp32) vec_doubles = std::max(vec_doubles, P.nnz);  // FP64 factorisation scratch
-  L.vec = take(vec_doubles * 8);
-  if (fp32) L.fvec = take(2 * n * 4);
-  if (is_isai(prec) && !fp32) L.tmpv = take(n * 8);
-  if (lu_prec && (fp32 || fast)) L.rinv = take(n * fts);
-  const int budget = (int)solve_max_smem();
-  // staging, most-reused operand first
-  if (lu_prec) {
-    if (prec == BILU_PRECOND_ILU0 || off + P.nnz * fts <= budget) L.F = take(P.nnz * fts);
-  } else if (is_isai(prec)) {
-    if (off + P.ail_rp[n] * fts <= budget) L.ail = take(P.ail_rp[n] * fts);
-    if (off + P.aiu_rp[n] * fts <= budget) L.aiu = take(P.aiu_rp[n] * fts);
-  }
-  if (off + P.nnz_in * 8 <= budget) L.A = take(P.nnz_in * 8);
-  L.total = off;
-  P.lay = L;
+  P.lay = layout_for(n, P.nnz_in, P.nnz, prec_kind(o.precond), is_fp32(o), o.reduction == BILU_REDUCE_FAST,
+                     P.has_isai ? P.ail_rp[n] : 0, P.has_isai ? P.aiu_rp[n] : 0, (int)solve_max_smem());
   int th = o.threads_per_system > 0 ? o.threads_per_system : round_up(std::max(n, 64), 32);
   th = std::min(round_up(std::max(th, 32), 32), 1024);
   P.threads = th;

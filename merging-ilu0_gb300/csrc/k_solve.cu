@@ -274,12 +274,14 @@ struct Scal {
   int status;  // BILU_SYS_*
 };
 
+// Solves system `sys` with the CTA: P = its pattern, lay = its shared-memory
+// carve-up, Ag / bg / xg = its values, right-hand side and solution, Fg / Lg /
+// Ug = its factors or ISAI values in global memory (when precomputed).
+// Block-wide: every thread of the CTA must call it.
 template <typename FT, bool REF, int S>
-__global__ void __launch_bounds__(1024) k_bicgstab(const SolveArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int sys = blockIdx.x;
-  if (sys >= a.nsys) return;
-  const DevPattern& P = a.pat;
+__device__ __forceinline__ void solve_one(const SolveArgs& a, const DevPattern& P, const SmemLayout& lay,
+                                          unsigned char* smem, const int sys, const double* Ag, const double* bg,
+                                          double* xg, const FT* Fg, const FT* Lg, const FT* Ug) {
   const int n = P.n, nnz = P.nnz, annz = P.a_nnz;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int* __restrict__ rp = P.a_rp;  // operator pattern
@@ -288,8 +290,8 @@ __global__ void __launch_bounds__(1024) k_bicgstab(const SolveArgs a) {
   constexpr bool kFP32 = sizeof(FT) == 4;
 
   // ---- shared-memory carve-up
-  Scal* sc = reinterpret_cast<Scal*>(smem + a.lay.red);
-  double* vec = reinterpret_cast<double*>(smem + a.lay.vec);
+  Scal* sc = reinterpret_cast<Scal*>(smem + lay.red);
+  double* vec = reinterpret_cast<double*>(smem + lay.vec);
   double* x = vec;
   double* r = vec + n;  // r, overwritten by s each half step
   double* rh = vec + 2 * n;
@@ -297,25 +299,23 @@ __global__ void __launch_bounds__(1024) k_bicgstab(const SolveArgs a) {
   double* v = vec + 4 * n;
   double* t = vec + 5 * n;
   double* ph = vec + 6 * n;  // p_hat, then s_hat
-  double* tmpv = a.lay.tmpv >= 0 ? reinterpret_cast<double*>(smem + a.lay.tmpv) : nullptr;
-  float* fy = a.lay.fvec >= 0 ? reinterpret_cast<float*>(smem + a.lay.fvec) : nullptr;
+  double* tmpv = lay.tmpv >= 0 ? reinterpret_cast<double*>(smem + lay.tmpv) : nullptr;
+  float* fy = lay.fvec >= 0 ? reinterpret_cast<float*>(smem + lay.fvec) : nullptr;
 
-  const double* Ag = a.A + (size_t)sys * annz;
   const double* Am = Ag;
-  if (a.lay.A >= 0) {
-    double* As = reinterpret_cast<double*>(smem + a.lay.A);
+  if (lay.A >= 0) {
+    double* As = reinterpret_cast<double*>(smem + lay.A);
     for (int k = tid; k < annz; k += nt) As[k] = __ldg(Ag + k);
     Am = As;
   }
-  const double* bg = a.b + (size_t)sys * n;
 
   // ---- preconditioner generation / staging
   const FT* F = nullptr;
   const FT* AIL = nullptr;
   const FT* AIU = nullptr;
-  void* rinv_raw = a.lay.rinv >= 0 ? (void*)(smem + a.lay.rinv) : nullptr;
+  void* rinv_raw = lay.rinv >= 0 ? (void*)(smem + lay.rinv) : nullptr;
   if (a.prec == PK_ILU_INKERNEL) {
-    FT* Fs = reinterpret_cast<FT*>(smem + a.lay.F);
+    FT* Fs = reinterpret_cast<FT*>(smem + lay.F);
     double* LUd = kFP32 ? vec : reinterpret_cast<double*>(Fs);
     __syncthreads();  // A staged
     for (int k = tid; k < nnz; k += nt) LUd[k] = Am[k];
@@ -327,26 +327,23 @@ __global__ void __launch_bounds__(1024) k_bicgstab(const SolveArgs a) {
     }
     F = Fs;
   } else if (a.prec == PK_LU_GLOBAL) {
-    const FT* Fg = reinterpret_cast<const FT*>(a.F) + (size_t)sys * nnz;
-    if (a.lay.F >= 0) {
-      FT* Fs = reinterpret_cast<FT*>(smem + a.lay.F);
+    if (lay.F >= 0) {
+      FT* Fs = reinterpret_cast<FT*>(smem + lay.F);
       for (int k = tid; k < nnz; k += nt) Fs[k] = Fg[k];
       F = Fs;
     } else {
       F = Fg;
     }
   } else if (a.prec == PK_ISAI) {
-    const FT* Lg = reinterpret_cast<const FT*>(a.ail) + (size_t)sys * P.ail_nnz;
-    const FT* Ug = reinterpret_cast<const FT*>(a.aiu) + (size_t)sys * P.aiu_nnz;
-    if (a.lay.ail >= 0) {
-      FT* s = reinterpret_cast<FT*>(smem + a.lay.ail);
+    if (lay.ail >= 0) {
+      FT* s = reinterpret_cast<FT*>(smem + lay.ail);
       for (int k = tid; k < P.ail_nnz; k += nt) s[k] = Lg[k];
       AIL = s;
     } else {
       AIL = Lg;
     }
-    if (a.lay.aiu >= 0) {
-      FT* s = reinterpret_cast<FT*>(smem + a.lay.aiu);
+    if (lay.aiu >= 0) {
+      FT* s = reinterpret_cast<FT*>(smem + lay.aiu);
       for (int k = tid; k < P.aiu_nnz; k += nt) s[k] = Ug[k];
       AIU = s;
     } else {
@@ -526,7 +523,6 @@ __global__ void __launch_bounds__(1024) k_bicgstab(const SolveArgs a) {
   __syncthreads();
 
   // ---- write back
-  double* xg = a.x + (size_t)sys * n;
   for (int i = tid; i < n; i += nt) xg[i] = x[i];
   if (tid == 0) {
     int st = sc->status;
@@ -547,6 +543,61 @@ __global__ void __launch_bounds__(1024) k_bicgstab(const SolveArgs a) {
   }
 }
 
+// One CTA per system of a batch sharing one pattern.
+template <typename FT, bool REF, int S>
+__global__ void __launch_bounds__(1024) k_bicgstab(const SolveArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sys = blockIdx.x;
+  if (sys >= a.nsys) return;
+  const DevPattern& P = a.pat;
+  solve_one<FT, REF, S>(a, P, a.lay, smem, sys, a.A + (size_t)sys * P.a_nnz, a.b + (size_t)sys * P.n,
+                        a.x + (size_t)sys * P.n,
+                        a.F ? reinterpret_cast<const FT*>(a.F) + (size_t)sys * P.nnz : nullptr,
+                        a.ail ? reinterpret_cast<const FT*>(a.ail) + (size_t)sys * P.ail_nnz : nullptr,
+                        a.aiu ? reinterpret_cast<const FT*>(a.aiu) + (size_t)sys * P.aiu_nnz : nullptr);
+}
+
+// Persistent CTAs over a work queue of systems with their own sizes and
+// patterns (one size bucket, longest systems first).  A CTA takes the next
+// queue position with one atomicAdd, solves that system with the merged
+// in-kernel ILU(0) and takes the next, until the queue is empty; there is no
+// waiting on other CTAs.
+template <typename FT, bool REF, int S>
+__global__ void __launch_bounds__(1024) k_bicgstab_uneven(const UnevenArgs u) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_job;
+  constexpr bool kFP32 = sizeof(FT) == 4;
+  for (;;) {
+    if (threadIdx.x == 0) s_job = atomicAdd(u.counter, 1);
+    __syncthreads();
+    const int job = s_job;
+    __syncthreads();
+    if (job >= u.count) break;
+    const int sys = __ldg(u.order + job);
+    const SysDesc d = u.desc[sys];
+    DevPattern P;
+    P.n = d.n;
+    P.nnz = P.a_nnz = d.nnz;
+    P.a_maxl = d.maxl;
+    P.rp = P.a_rp = u.meta + d.o_rp;
+    P.ci = P.a_ci = u.meta + d.o_ci;
+    P.diag = u.meta + d.o_diag;
+    P.nlev_lo = d.nlev_lo;
+    P.nlev_up = d.nlev_up;
+    P.maxw_lo = P.maxw_up = d.maxw;
+    P.lev_lo_ptr = u.meta + d.o_llp;
+    P.lev_lo_rows = u.meta + d.o_llr;
+    P.lev_up_ptr = u.meta + d.o_lup;
+    P.lev_up_rows = u.meta + d.o_lur;
+    P.dep_ptr = u.meta + d.o_dp;
+    P.dep = reinterpret_cast<const int2*>(u.meta + d.o_dep);
+    const SmemLayout lay = layout_for(d.n, d.nnz, d.nnz, u.base.prec, kFP32, !REF, 0, 0, u.smem_budget);
+    solve_one<FT, REF, S>(u.base, P, lay, smem, sys, u.base.A + d.val_off, u.base.b + d.vec_off,
+                          u.base.x + d.vec_off, nullptr, nullptr, nullptr);
+    __syncthreads();
+  }
+}
+
 template <typename FT, bool REF>
 cudaError_t launch_t(const SolveArgs& a, int threads, int maxl, cudaStream_t st) {
   void (*kern)(const SolveArgs);
@@ -563,6 +614,26 @@ cudaError_t launch_t(const SolveArgs& a, int threads, int maxl, cudaStream_t st)
 }
 
 }  // namespace
+
+template <typename FT, bool REF>
+void* uneven_kernel_t(int maxl) {
+  if (maxl <= 8) return (void*)k_bicgstab_uneven<FT, REF, 8>;
+  if (maxl <= 16) return (void*)k_bicgstab_uneven<FT, REF, 16>;
+  return (void*)k_bicgstab_uneven<FT, REF, 32>;
+}
+
+void* uneven_kernel(int fp32, int reduce_fast, int maxl) {
+  if (fp32) return reduce_fast ? uneven_kernel_t<float, false>(maxl) : uneven_kernel_t<float, true>(maxl);
+  return reduce_fast ? uneven_kernel_t<double, false>(maxl) : uneven_kernel_t<double, true>(maxl);
+}
+
+cudaError_t launch_uneven(const UnevenArgs& u, int threads, int grid, int fp32, int reduce_fast, int maxl,
+                          cudaStream_t st) {
+  if (u.count == 0 || grid == 0) return cudaSuccess;
+  void* k = uneven_kernel(fp32, reduce_fast, maxl);
+  void* args[] = {const_cast<UnevenArgs*>(&u)};
+  return cudaLaunchKernel(k, dim3(grid), dim3(threads), args, (size_t)u.smem_budget, st);
+}
 
 cudaError_t launch_solve(const SolveArgs& a, int threads, int fp32, int reduce_fast, int maxl, cudaStream_t st) {
   if (a.nsys == 0) return cudaSuccess;

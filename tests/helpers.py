@@ -96,3 +96,27 @@ def assert_bitwise(a, b, what):
         idx = np.argwhere(~same)[:5]
         raise AssertionError(f"{what}: {int((~same).sum())} of {a.size} differ, first at {idx.tolist()}: "
                              f"{a[tuple(idx[0])]!r} vs {b[tuple(idx[0])]!r}")
+
+
+def uneven_split(sn, sz, rp, ci, v, b):
+    """Per-system views (row_ptrs, col_idxs, values, b) of a concatenated uneven batch."""
+    out = []
+    ro = zo = 0
+    for s in range(len(sn)):
+        n, nz = int(sn[s]), int(sz[s])
+        out.append((rp[ro + s: ro + s + n + 1], ci[zo: zo + nz], v[zo: zo + nz], b[ro: ro + n]))
+        ro += n
+        zo += nz
+    return out
+
+
+def oracle_uneven(sn, sz, rp, ci, v, b, precond=0, approach=1, tol_mode=0, tol=1e-11, max_iter=500, fp32=False):
+    """Oracle per system (each its own pattern); concatenated outputs."""
+    xs, its, cvs, rss, trs, sts = [], [], [], [], [], []
+    for (r, c, vv, bb) in uneven_split(sn, sz, rp, ci, v, b):
+        o = oracle_pipeline(r, c, vv[None, :], bb[None, :], precond, approach=approach, tol_mode=tol_mode, tol=tol,
+                            max_iter=max_iter, fp32=fp32)
+        xs.append(o["x"][0]); its.append(o["iters"][0]); cvs.append(o["conv"][0]); rss.append(o["res"][0])
+        trs.append(o["true_res"][0]); sts.append(o["status"][0])
+    return {"x": np.concatenate(xs), "iters": np.array(its, np.float32), "conv": np.array(cvs, np.int32),
+            "res": np.array(rss), "true_res": np.array(trs), "status": np.array(sts, np.int32)}
