@@ -38,7 +38,7 @@ HEADLINE = dict(name="parilu5_isai_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsy
                 desc="ParILU(0) 5 sweeps + ISAI(L,U on |T|^2) BiCGSTAB, 4096 FP64 systems, 3D 7-point 10x10x10 "
                      "(n=1000, nnz=6400), Peclet skew U(0,0.5), rel. tol 1e-10, max 500 iterations",
                 opts=dict(precond=4, parilu_sweeps=5, isai_power=2, tol_mode=1, tol=1e-10, max_iter=500,
-                          reduction=1, factor_precision=0))
+                          reduction=1, factor_precision=0), fwd_sample=32)
 SECONDARY = [
     dict(name="plain_ilu0_2d5_16x16_fast", kind=1, grid=(16, 16, 1), nsys=16384,
          desc="plain form: merged ILU(0) BiCGSTAB, 16384 FP64 systems, 2D 5-point 16x16, rel 1e-10, FAST order",
@@ -48,10 +48,10 @@ SECONDARY = [
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=0)),
     dict(name="fp32_ilu0_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768,
          desc="FP32-stored ILU(0) factors (FP64 recurrences), 32768 convection-diffusion systems 24x24",
-         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1)),
+         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1), fwd_sample=256),
     dict(name="fp64_ilu0_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768,
          desc="same workload with FP64 factors",
-         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=0)),
+         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=0), fwd_sample=256),
 ]
 
 
@@ -200,6 +200,12 @@ def measure(wl, steps, warmup, dev, stream, sampler=None, e2e=False, timed_hook=
         if timed_hook:
             timed_hook("end")
         ms = e0.elapsed_time(e1)
+    fwd = None
+    if wl.get("fwd_sample"):
+        ids = np.arange(0, nsys, max(1, nsys // wl["fwd_sample"]), dtype=np.int32)[: wl["fwd_sample"]]
+        fe = plan.forward_error(V, B, X, ids)
+        fwd = {"systems": len(ids), "median": float(np.median(fe)), "max": float(fe.max()),
+               "oracle": "FP64 dense LU with partial pivoting on the GPU (bilu_forward_error)"}
     iters = it.cpu().numpy()
     conv = cv.cpu().numpy()
     trn = tr.cpu().numpy()
@@ -209,7 +215,7 @@ def measure(wl, steps, warmup, dev, stream, sampler=None, e2e=False, timed_hook=
            "systems_per_s": nsys * steps / (ms / 1e3), "setup_ms": statistics.mean(setup),
            "solve_ms": statistics.mean(solve), "mean_iters": float(iters.mean()), "max_iters": float(iters.max()),
            "converged": int((conv == 1).sum()), "max_rel_true_res": float((trn / bn).max()), "info": info,
-           "clocks": clocks}
+           "clocks": clocks, "forward_error": fwd}
     if e2e:
         # end to end through the C ABI with host buffers: H2D of values and b, solve, D2H of x and results
         hv = torch.empty(V.shape, dtype=V.dtype, pin_memory=True)
@@ -343,7 +349,8 @@ def main():
             try:
                 r = measure(wl, 2, 1, dev, stream)
                 secondary.append({k: r[k] for k in ("name", "nsys", "systems_per_s", "setup_ms", "solve_ms",
-                                                    "mean_iters", "converged", "max_rel_true_res")} |
+                                                    "mean_iters", "converged", "max_rel_true_res",
+                                                    "forward_error")} |
                                  {"workload": wl["desc"]})
             except Exception as ex:  # a secondary workload never hides the headline
                 secondary.append({"name": wl["name"], "error": str(ex)})
@@ -385,7 +392,8 @@ def main():
                           "note": "FP64 issue, not HBM, bounds this kernel on GB300"},
         "stages_ms": {"setup": res["setup_ms"], "solve": res["solve_ms"]},
         "solve_quality": {"mean_iters": res["mean_iters"], "max_iters": res["max_iters"],
-                          "converged": res["converged"], "max_rel_true_residual": res["max_rel_true_res"]},
+                          "converged": res["converged"], "max_rel_true_residual": res["max_rel_true_res"],
+                          "forward_error": res["forward_error"]},
         "cpu_baseline": {"value": rate, "unit": "systems/s", "cores": used, "kind": "port",
                          "sample": f"{cpu_sample} systems of the headline workload through the CPU restatement "
                                    f"({dt:.2f} s, {used} OpenMP threads of {cores} host cores)"},

@@ -264,6 +264,16 @@ bilu_status bilu_uneven_solve(bilu_uneven_plan* plan, const double* d_values, co
 bilu_status bilu_uneven_get_info(const bilu_uneven_plan* plan, int bucket, int* n_lo, int* n_hi, int* systems,
                                  int* threads, int* grid, int* smem_bytes, float* tuned_ms);
 
+/* Forward error against an FP64 dense LU with partial pivoting (no reference
+ * counterpart): for each sampled system s = h_sys_ids[q], the dense solution
+ * x_dense of A_s x = b_s and h_fwd_err[q] = ||x_s - x_dense||_2 / ||x_dense||_2
+ * (d_x may be NULL: then the errors are ||x_dense||).  d_x_dense (nsample*n,
+ * optional) receives the dense solutions.  Allocates n*n doubles per sampled
+ * system and synchronises the stream. */
+bilu_status bilu_forward_error(const bilu_plan* plan, int nsample, const int* h_sys_ids, const double* d_values,
+                               const double* d_b, const double* d_x, double* h_fwd_err, double* d_x_dense,
+                               void* stream);
+
 /* ---------------------------------------------------------------- misc */
 const char* bilu_last_error(void);
 const char* bilu_version(void);

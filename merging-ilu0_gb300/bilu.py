@@ -31,7 +31,7 @@ EXPORTED = [
     "bilu_parilu0", "bilu_split_lu", "bilu_isai", "bilu_true_residual", "bilu_last_error",
     "bilu_version", "bilu_device_count", "bilu_gen_stencil", "bilu_gen_uneven", "bilu_plan_enable_timing",
     "bilu_plan_last_timing", "bilu_solve_noalloc", "bilu_uneven_plan_create", "bilu_uneven_plan_destroy",
-    "bilu_uneven_autotune", "bilu_uneven_solve", "bilu_uneven_get_info",
+    "bilu_uneven_autotune", "bilu_uneven_solve", "bilu_uneven_get_info", "bilu_forward_error",
 ]
 
 
@@ -97,6 +97,7 @@ def lib():
         L.bilu_uneven_autotune.argtypes = [vp, vp, vp, vp, vp]
         L.bilu_uneven_solve.argtypes = [vp, vp, vp, vp, C.POINTER(Results), vp]
         L.bilu_uneven_get_info.argtypes = [vp, i, ip, ip, ip, ip, ip, ip, C.POINTER(C.c_float)]
+        L.bilu_forward_error.argtypes = [vp, i, ip, vp, vp, vp, C.POINTER(d), vp, vp]
         L.bilu_plan_enable_timing.argtypes = [vp, i]
         L.bilu_plan_last_timing.argtypes = [vp, C.POINTER(Timing)]
         L.bilu_gen_uneven.argtypes = [i, C.c_uint64, i, i, i, i, ip, ip, ip, ip, C.POINTER(d), C.POINTER(d)]
@@ -317,6 +318,14 @@ class Plan:
     def true_residual(self, values, b, x, out, stream=None):
         _check(lib().bilu_true_residual(self.h, b.shape[0], _dev(values), _dev(b), _dev(x), _dev(out),
                                         _stream(stream)))
+
+    def forward_error(self, values, b, x, sys_ids, x_dense=None, stream=None):
+        """||x_s - x_dense||_2 / ||x_dense||_2 for the sampled systems (FP64 dense LU on the GPU)."""
+        ids = np.ascontiguousarray(sys_ids, np.int32)
+        out = np.zeros(len(ids))
+        _check(lib().bilu_forward_error(self.h, len(ids), _iptr(ids), _dev(values), _dev(b), _dev(x), _dptr(out),
+                                        _dev(x_dense), _stream(stream)))
+        return out
 
     def expand_values(self, vin, vout, stream=None):
         _check(lib().bilu_expand_values(self.h, vin.shape[0], _dev(vin), _dev(vout), _stream(stream)))

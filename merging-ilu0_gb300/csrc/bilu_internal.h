@@ -178,6 +178,8 @@ cudaError_t launch_parilu0(const DevPattern& p, int nsys, const double* A, const
                            int sweeps, int threads, cudaStream_t st);
 cudaError_t launch_isai(const DevPattern& p, int nsys, const double* lu, void* ail, void* aiu, int fp32,
                         int threads, cudaStream_t st);
+cudaError_t launch_dense_solve(const DevPattern& p, int nsample, const int* sys_ids, const double* A, const double* b,
+                               double* work, double* x_out, cudaStream_t st);
 cudaError_t launch_to_float(const double* a, float* b, size_t n, cudaStream_t st);
 cudaError_t launch_split(const DevPattern& p, int nsys, const double* lu, double* L, double* U, cudaStream_t st);
 cudaError_t launch_true_residual(const DevPattern& p, int nsys, const double* A, const double* b, const double* x,

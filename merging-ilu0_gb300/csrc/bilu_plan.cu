@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -765,3 +766,44 @@ bilu_status bilu_true_residual(const bilu_plan* P, int nsys, const double* d_val
 }
 
 }  // extern "C"
+
+extern "C" bilu_status bilu_forward_error(const bilu_plan* P, int nsample, const int* h_sys_ids, const double* d_values,
+                                          const double* d_b, const double* d_x, double* h_fwd_err, double* d_x_dense,
+                                          void* stream) {
+  if (!P || nsample < 0 || (nsample > 0 && (!h_sys_ids || !d_values || !d_b || !h_fwd_err)))
+    return set_error(BILU_ERR_INVALID, "bilu_forward_error: bad arguments");
+  if (nsample == 0) return BILU_OK;
+  const int n = P->n;
+  cudaStream_t st = (cudaStream_t)stream;
+  int* ids = nullptr;
+  double* work = nullptr;
+  double* xd = nullptr;
+  const size_t per = (size_t)n * n + n;
+  cudaError_t e = cudaMalloc((void**)&ids, sizeof(int) * nsample);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&work, sizeof(double) * per * nsample);
+  if (e == cudaSuccess && !d_x_dense) e = cudaMalloc((void**)&xd, sizeof(double) * (size_t)n * nsample);
+  double* xout = d_x_dense ? d_x_dense : xd;
+  std::vector<double> hx((size_t)n * nsample), hs((size_t)n * nsample);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ids, h_sys_ids, sizeof(int) * nsample, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = launch_dense_solve(P->dp, nsample, ids, d_values, d_b, work, xout, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hx.data(), xout, sizeof(double) * hx.size(), cudaMemcpyDeviceToHost, st);
+  for (int q = 0; q < nsample && e == cudaSuccess && d_x; ++q)
+    e = cudaMemcpyAsync(hs.data() + (size_t)q * n, d_x + (size_t)h_sys_ids[q] * n, sizeof(double) * n,
+                        cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(ids);
+  cudaFree(work);
+  cudaFree(xd);
+  if (e != cudaSuccess) return cuda_err(e, "forward error");
+  for (int q = 0; q < nsample; ++q) {
+    double num = 0.0, den = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double xe = hx[(size_t)q * n + i];
+      const double dx = (d_x ? hs[(size_t)q * n + i] : 0.0) - xe;
+      num += dx * dx;
+      den += xe * xe;
+    }
+    h_fwd_err[q] = den > 0.0 ? std::sqrt(num / den) : std::sqrt(num);
+  }
+  return BILU_OK;
+}

@@ -612,7 +612,10 @@ ORC_API void orc_true_residual(int n, int nnz, const int* rp, const int* ci, int
 
 // ===========================================================================
 // FP64 dense LU with partial pivoting (forward-error oracle; no reference
-// counterpart).  Solves each system densely; returns x.
+// counterpart).  Solves each system densely; returns x.  Pivot = first row
+// of largest |a_ik|; multipliers f = a_ik / a_kk; updates fma(-f, a_kj, a_ij)
+// (rhs alike); column-oriented back substitution.  The library's GPU dense
+// solve (bilu_forward_error) performs the same operations.
 // ===========================================================================
 ORC_API void orc_dense_solve(int n, int nnz, const int* rp, const int* ci, int nsys, const int* sys_ids,
                              const double* A, const double* b, double* x_out) {
@@ -647,11 +650,11 @@ ORC_API void orc_dense_solve(int n, int nnz, const int* rp, const int* ci, int n
         y[i] = std::fma(-f, y[k], y[i]);
       }
     }
+    // column-oriented back substitution: x_j = y_j / u_jj, then y_i -= u_ij x_j for i < j
     double* xs = x_out + (size_t)q * n;
-    for (int i = n - 1; i >= 0; --i) {
-      double acc = y[i];
-      for (int j = i + 1; j < n; ++j) acc = std::fma(-M[(size_t)i * n + j], xs[j], acc);
-      xs[i] = acc / M[(size_t)i * n + i];
+    for (int j = n - 1; j >= 0; --j) {
+      xs[j] = y[j] / M[(size_t)j * n + j];
+      for (int i = 0; i < j; ++i) y[i] = std::fma(-M[(size_t)i * n + j], xs[j], y[i]);
     }
   }
 }

@@ -212,3 +212,24 @@ def test_nonfinite_status(cuda):
     g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0, max_iter=50)
     assert g["conv"][2] == -1 and g["status"][2] == bilu.SYS_NONFINITE
     assert np.all(g["conv"][[0, 1, 3]] == 1)
+
+
+# ---------------------------------------------------------------- forward error
+@pytest.mark.parametrize("family", ["2d5_8x8", "cd2d_12x12", "3d7_5x5x5"])
+def test_dense_lu_bitwise_and_forward_error(cuda, family):
+    import torch
+    rp, ci, v, b = H.workload(family, 16)
+    ids = np.array([0, 3, 7, 15], np.int32)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0, tol_mode=bilu.TOL_REL, tol=1e-10)
+    with bilu.Plan(rp, ci) as plan:
+        V = torch.from_numpy(v).to(cuda)
+        B = torch.from_numpy(b).to(cuda)
+        X = torch.from_numpy(g["x"]).to(cuda)
+        XD = torch.empty((len(ids), b.shape[1]), dtype=torch.float64, device=cuda)
+        fe = plan.forward_error(V, B, X, ids, x_dense=XD)
+        torch.cuda.synchronize()
+    xd = O.dense_solve(rp, ci, v, b, ids)
+    H.assert_bitwise(XD.cpu().numpy(), xd, f"GPU dense LU vs oracle {family}")
+    ref = np.linalg.norm(g["x"][ids] - xd, axis=1) / np.linalg.norm(xd, axis=1)
+    np.testing.assert_allclose(fe, ref, rtol=1e-12, atol=1e-30)
+    assert np.all(fe < 1e-8)
