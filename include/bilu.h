@@ -91,6 +91,9 @@ typedef struct bilu_options {
   int    reduction;          /* BILU_REDUCE_REF | BILU_REDUCE_FAST                          */
   int    compute_true_residual; /* nonzero: fill bilu_results.true_res_norms              */
   int    threads_per_system; /* 0 = automatic; otherwise CTA size used per system           */
+  double parilu_res_tol;     /* > 0: ParILU sweeps stop once the ILU residual
+                                ||(A - LU)|_S||_F / ||A||_F <= parilu_res_tol (at most
+                                parilu_sweeps sweeps); 0: exactly parilu_sweeps sweeps     */
 } bilu_options;
 
 /* Fills *opts with the reference defaults: merged ILU(0), approach 1, 5 sweeps,
@@ -106,6 +109,8 @@ typedef struct bilu_results {
   double* iter_res_norms;  /* recursive residual norm at exit                                 */
   double* true_res_norms;  /* ||b - A x||_2 computed after the solve                          */
   int*    status;          /* BILU_SYS_* detailed outcome                                     */
+  int*    parilu_sweeps;   /* ParILU preconditioners: sweeps performed                        */
+  double* ilu_residual;    /* ParILU preconditioners: ILU residual of the factors used       */
 } bilu_results;
 
 /* ---------------------------------------------------------------- plans */
@@ -273,6 +278,51 @@ bilu_status bilu_uneven_get_info(const bilu_uneven_plan* plan, int bucket, int* 
 bilu_status bilu_forward_error(const bilu_plan* plan, int nsample, const int* h_sys_ids, const double* d_values,
                                const double* d_b, const double* d_x, double* h_fwd_err, double* d_x_dense,
                                void* stream);
+
+/* ---------------------------------------------------------------- learned ParILU warm start */
+/* A per-nonzero MLP (9 features -> 64 -> 64 -> 1, GELU, BF16 weights, FP32
+ * accumulation) predicting the converged ParILU(0) factors from the matrix
+ * values; no counterpart in the reference.  Features of entry (i,j), scaled
+ * by |a_ii|: a_ij, a_ii, a_jj, ||A(i,:)||, ||A(:,j)||, level(i), sign(j-i),
+ * and the first-order Schur corrections c_i, c_j (c_r = sum_{k<r} a_rk a_kr / a_kk).
+ * The network outputs a relative correction y of the first-order factor
+ * estimate; warm start lu0_ij = a_ij * base_ij * (1 + y).  Entries on or
+ * above the diagonal without dependency pairs converge to a_ij exactly and are
+ * copied instead.  Inference runs the 64x64 layer on the tensor cores.
+ * Values are in the plan's factor pattern (the plan must have every diagonal). */
+typedef struct bilu_mlp bilu_mlp;
+bilu_status bilu_mlp_create(bilu_mlp** mlp, uint64_t seed);
+bilu_status bilu_mlp_destroy(bilu_mlp* mlp);
+int bilu_mlp_param_count(void);
+/* FP32 master parameters: W1[64][9], b1[64], W2[64][64], b2[64], W3[64], b3. */
+bilu_status bilu_mlp_get_params(const bilu_mlp* mlp, float* h_params);
+bilu_status bilu_mlp_set_params(bilu_mlp* mlp, const float* h_params);
+/* `steps` Adam steps (learning rate decaying from lr to lr/20 on a cosine;
+ * beta 0.9 / 0.999) on random minibatches of `batch` nonzeros drawn from the
+ * nsys systems (d_lu_target: their converged ParILU factors), among the
+ * entries the network predicts; mean squared error of the factor correction.  Synchronises;
+ * h_losses (steps entries, optional) receives the per-step loss. */
+bilu_status bilu_mlp_train(bilu_mlp* mlp, const bilu_plan* plan, int nsys, const double* d_values,
+                           const double* d_lu_target, int steps, int batch, float lr, uint64_t seed,
+                           float* h_losses, void* stream);
+/* Loss and gradient (not applied) over the given global entries
+ * (s * nnz + e); synchronises.  For checking the backward pass. */
+bilu_status bilu_mlp_loss_grad(bilu_mlp* mlp, const bilu_plan* plan, int nsys, const double* d_values,
+                               const double* d_lu_target, int nsample, const int* h_idx, float* h_loss,
+                               float* h_grad, void* stream);
+/* Features (nsample * 9), network outputs and first-order estimates of the
+ * given entries; synchronises.  For checking the forward pass. */
+bilu_status bilu_mlp_eval(bilu_mlp* mlp, const bilu_plan* plan, int nsys, const double* d_values, int nsample,
+                          const int* h_idx, float* h_features, float* h_out, double* h_base, void* stream);
+/* Warm start of every system: the network's factors, or A itself where their
+ * ILU residual ||(A - L0 U0)|_S||_F / ||A||_F exceeds `threshold`.  Optional
+ * device outputs: the residual and 1 / 0 for warm start used / fallback.
+ * d_lu0 feeds bilu_solve_warm or bilu_parilu0. */
+bilu_status bilu_mlp_warm_start(bilu_mlp* mlp, const bilu_plan* plan, int nsys, const double* d_values,
+                                double* d_lu0, double threshold, double* d_ilu_res, int* d_used, void* stream);
+/* Flat binary file: "BILUMLP1", three ints (features, hidden, params), FP32 parameters. */
+bilu_status bilu_mlp_save(const bilu_mlp* mlp, const char* path);
+bilu_status bilu_mlp_load(bilu_mlp* mlp, const char* path);
 
 /* ---------------------------------------------------------------- misc */
 const char* bilu_last_error(void);

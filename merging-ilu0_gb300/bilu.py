@@ -32,6 +32,8 @@ EXPORTED = [
     "bilu_version", "bilu_device_count", "bilu_gen_stencil", "bilu_gen_uneven", "bilu_plan_enable_timing",
     "bilu_plan_last_timing", "bilu_solve_noalloc", "bilu_uneven_plan_create", "bilu_uneven_plan_destroy",
     "bilu_uneven_autotune", "bilu_uneven_solve", "bilu_uneven_get_info", "bilu_forward_error",
+    "bilu_mlp_create", "bilu_mlp_destroy", "bilu_mlp_param_count", "bilu_mlp_get_params", "bilu_mlp_set_params",
+    "bilu_mlp_train", "bilu_mlp_loss_grad", "bilu_mlp_eval", "bilu_mlp_warm_start", "bilu_mlp_save", "bilu_mlp_load",
 ]
 
 
@@ -40,12 +42,14 @@ class Options(C.Structure):
         ("precond", C.c_int), ("ilu_approach", C.c_int), ("parilu_sweeps", C.c_int), ("isai_power", C.c_int),
         ("tol_mode", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int), ("factor_precision", C.c_int),
         ("reduction", C.c_int), ("compute_true_residual", C.c_int), ("threads_per_system", C.c_int),
+        ("parilu_res_tol", C.c_double),
     ]
 
 
 class Results(C.Structure):
     _fields_ = [("iter_counts", C.c_void_p), ("conv_flags", C.c_void_p), ("iter_res_norms", C.c_void_p),
-                ("true_res_norms", C.c_void_p), ("status", C.c_void_p)]
+                ("true_res_norms", C.c_void_p), ("status", C.c_void_p), ("parilu_sweeps", C.c_void_p),
+                ("ilu_residual", C.c_void_p)]
 
 
 class PlanInfo(C.Structure):
@@ -98,6 +102,18 @@ def lib():
         L.bilu_uneven_solve.argtypes = [vp, vp, vp, vp, C.POINTER(Results), vp]
         L.bilu_uneven_get_info.argtypes = [vp, i, ip, ip, ip, ip, ip, ip, C.POINTER(C.c_float)]
         L.bilu_forward_error.argtypes = [vp, i, ip, vp, vp, vp, C.POINTER(d), vp, vp]
+        fp = C.POINTER(C.c_float)
+        L.bilu_mlp_create.argtypes = [C.POINTER(vp), C.c_uint64]
+        L.bilu_mlp_destroy.argtypes = [vp]
+        L.bilu_mlp_param_count.restype = i
+        L.bilu_mlp_get_params.argtypes = [vp, fp]
+        L.bilu_mlp_set_params.argtypes = [vp, fp]
+        L.bilu_mlp_train.argtypes = [vp, vp, i, vp, vp, i, i, C.c_float, C.c_uint64, fp, vp]
+        L.bilu_mlp_loss_grad.argtypes = [vp, vp, i, vp, vp, i, ip, fp, fp, vp]
+        L.bilu_mlp_eval.argtypes = [vp, vp, i, vp, i, ip, fp, fp, C.POINTER(d), vp]
+        L.bilu_mlp_warm_start.argtypes = [vp, vp, i, vp, vp, d, vp, vp, vp]
+        L.bilu_mlp_save.argtypes = [vp, C.c_char_p]
+        L.bilu_mlp_load.argtypes = [vp, C.c_char_p]
         L.bilu_plan_enable_timing.argtypes = [vp, i]
         L.bilu_plan_last_timing.argtypes = [vp, C.POINTER(Timing)]
         L.bilu_gen_uneven.argtypes = [i, C.c_uint64, i, i, i, i, ip, ip, ip, ip, C.POINTER(d), C.POINTER(d)]
@@ -272,12 +288,12 @@ class Plan:
         return rp, ci[: nnz.value]
 
     def solve(self, values, b, x, iters=None, conv=None, res=None, true_res=None, status=None, stream=None,
-              lu_init=None):
+              lu_init=None, sweeps=None, ilu_res=None):
         """All arguments are CUDA tensors (values nsys*nnz_in f64, b/x nsys*n f64, iters f32, conv/status i32,
-        res/true_res f64); returns immediately (stream ordered)."""
+        res/true_res f64, sweeps i32, ilu_res f64); returns immediately (stream ordered)."""
         nsys = b.shape[0] if b.dim() > 1 else b.numel() // self.n
         R = Results(*(C.c_void_p(t.data_ptr()) if t is not None else None
-                      for t in (iters, conv, res, true_res, status)))
+                      for t in (iters, conv, res, true_res, status, sweeps, ilu_res)))
         if lu_init is None:
             _check(lib().bilu_solve(self.h, nsys, _dev(values), _dev(b), _dev(x), C.byref(R), _stream(stream)))
         else:
@@ -305,7 +321,7 @@ class Plan:
         nsys = values.shape[0]
         _check(lib().bilu_ilu0(self.h, nsys, _dev(values), _dev(lu), approach, _stream(stream)))
 
-    def parilu0(self, values, lu, sweeps, init=None, stream=None):
+    def parilu0(self, values, lu, sweeps, init=None, stream=None):  # noqa: D401
         nsys = values.shape[0]
         _check(lib().bilu_parilu0(self.h, nsys, _dev(values), _dev(init), _dev(lu), sweeps, _stream(stream)))
 
@@ -329,3 +345,77 @@ class Plan:
 
     def expand_values(self, vin, vout, stream=None):
         _check(lib().bilu_expand_values(self.h, vin.shape[0], _dev(vin), _dev(vout), _stream(stream)))
+
+
+def _fptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Mlp:
+    """The learned ParILU warm start (bilu_mlp_*)."""
+
+    def __init__(self, seed=1):
+        h = C.c_void_p()
+        _check(lib().bilu_mlp_create(C.byref(h), seed))
+        self.h = h
+        self.nparams = lib().bilu_mlp_param_count()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().bilu_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def params(self):
+        p = np.zeros(self.nparams, np.float32)
+        _check(lib().bilu_mlp_get_params(self.h, _fptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        _check(lib().bilu_mlp_set_params(self.h, _fptr(p)))
+
+    def train(self, plan, values, lu_target, steps, batch, lr, seed=0, stream=None):
+        losses = np.zeros(max(steps, 1), np.float32)
+        _check(lib().bilu_mlp_train(self.h, plan.h, values.shape[0], _dev(values), _dev(lu_target), steps, batch,
+                                    C.c_float(lr), seed, _fptr(losses), _stream(stream)))
+        return losses[:steps]
+
+    def loss_grad(self, plan, values, lu_target, idx, stream=None):
+        idx = np.ascontiguousarray(idx, np.int32)
+        loss = np.zeros(1, np.float32)
+        grad = np.zeros(self.nparams, np.float32)
+        _check(lib().bilu_mlp_loss_grad(self.h, plan.h, values.shape[0], _dev(values), _dev(lu_target), len(idx),
+                                        _iptr(idx), _fptr(loss), _fptr(grad), _stream(stream)))
+        return float(loss[0]), grad
+
+    def eval(self, plan, values, idx, stream=None):
+        idx = np.ascontiguousarray(idx, np.int32)
+        feat = np.zeros((len(idx), 9), np.float32)
+        out = np.zeros(len(idx), np.float32)
+        base = np.zeros(len(idx))
+        _check(lib().bilu_mlp_eval(self.h, plan.h, values.shape[0], _dev(values), len(idx), _iptr(idx), _fptr(feat),
+                                   _fptr(out), _dptr(base), _stream(stream)))
+        return feat, out, base
+
+    def warm_start(self, plan, values, lu0, threshold=1e-3, ilu_res=None, used=None, stream=None):
+        _check(lib().bilu_mlp_warm_start(self.h, plan.h, values.shape[0], _dev(values), _dev(lu0),
+                                         C.c_double(threshold), _dev(ilu_res), _dev(used), _stream(stream)))
+
+    def save(self, path):
+        _check(lib().bilu_mlp_save(self.h, path.encode()))
+
+    def load(self, path):
+        _check(lib().bilu_mlp_load(self.h, path.encode()))
+

@@ -12,6 +12,11 @@
 
 namespace bilu {
 
+// learned warm start: 9 features -> 64 -> 64 -> 1
+constexpr int kMlpFeatures = 9;
+constexpr int kMlpHidden = 64;
+constexpr int kMlpParams = kMlpHidden * kMlpFeatures + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;
+
 // Records the message for bilu_last_error() and returns the code.
 bilu_status set_error(bilu_status code, const std::string& msg);
 
@@ -63,6 +68,13 @@ struct DevPattern {
   int nnz_L = 0, nnz_U = 0;
   const int* l_src = nullptr;
   const int* u_src = nullptr;
+  // per row: lower-solve level; per entry: position of the transposed entry or -1
+  const int* row_lev = nullptr;
+  const int* tpos = nullptr;
+  // entries whose converged ParILU value is not simply a_ij (all but the upper
+  // entries without dependency pairs): the ones the learned warm start predicts
+  int n_mlp = 0;
+  const int* mlp_ent = nullptr;
 };
 
 // Shared-memory carve-up of the solver kernel for one system (byte offsets;
@@ -175,11 +187,27 @@ cudaError_t launch_expand(const DevPattern& p, int nsys, const double* vin, doub
 cudaError_t launch_ilu0(const DevPattern& p, int nsys, const double* A, double* lu, int approach, int threads,
                         cudaStream_t st);
 cudaError_t launch_parilu0(const DevPattern& p, int nsys, const double* A, const double* init, double* lu,
-                           int sweeps, int threads, cudaStream_t st);
+                           int sweeps, int threads, cudaStream_t st, double res_tol = 0.0, int* sweeps_out = nullptr,
+                           double* res_out = nullptr, int fast = 0);
 cudaError_t launch_isai(const DevPattern& p, int nsys, const double* lu, void* ail, void* aiu, int fp32,
                         int threads, cudaStream_t st);
 cudaError_t launch_dense_solve(const DevPattern& p, int nsample, const int* sys_ids, const double* A, const double* b,
                                double* work, double* x_out, cudaStream_t st);
+cudaError_t launch_mlp_rowstats(const DevPattern& p, int nsys, const double* A, float* rown, float* coln, float* corr,
+                                cudaStream_t st);
+size_t mlp_train_smem();
+cudaError_t launch_mlp_train(const DevPattern& p, int nsys, const double* A, const double* LUt, const float* rown,
+                             const float* coln, const float* corr, const void* pbf, int nsample, const int* idx,
+                             uint64_t seed, float* grad, float* loss, cudaStream_t st);
+cudaError_t launch_mlp_adam(float* p, float* m, float* v, const float* g, void* pbf, int count, float lr, int step,
+                            cudaStream_t st);
+cudaError_t launch_mlp_to_bf16(const float* p, void* pbf, int count, cudaStream_t st);
+cudaError_t launch_mlp_eval(const DevPattern& p, int nsys, const double* A, const float* rown, const float* coln,
+                            const float* corr, const void* pbf, int nsample, const int* idx, float* feat, float* out,
+                            double* base, cudaStream_t st);
+cudaError_t launch_mlp_warm(const DevPattern& p, int nsys, const double* A, const float* rown, const float* coln,
+                            const float* corr, const void* pbf, double threshold, double* lu0, double* res, int* used,
+                            cudaStream_t st);
 cudaError_t launch_to_float(const double* a, float* b, size_t n, cudaStream_t st);
 cudaError_t launch_split(const DevPattern& p, int nsys, const double* lu, double* L, double* U, cudaStream_t st);
 cudaError_t launch_true_residual(const DevPattern& p, int nsys, const double* A, const double* b, const double* x,
@@ -199,6 +227,7 @@ struct bilu_plan {
   std::vector<int> dep_ptr;
   std::vector<int> dep;  // pairs
   std::vector<int> l_rp, l_ci, l_src, u_rp, u_ci, u_src;
+  std::vector<int> row_lev, tpos, mlp_ent;
   bool has_isai = false;
   std::vector<int> ail_rp, ail_ci, aiu_rp, aiu_ci;
   std::vector<int> ail_prog_ptr, ail_prog, aiu_prog_ptr, aiu_prog;  // prog in int units (pairs)

@@ -148,7 +148,9 @@ extern "C" bilu_status bilu_solve_noalloc(bilu_plan* P, int nsys, const double* 
     if (prec == BILU_PRECOND_ILU0_SPLIT || prec == BILU_PRECOND_ILU0_ISAI)
       e = launch_ilu0(P->dp, nsys, fv, lu, o.ilu_approach, ft, s);
     else
-      e = launch_parilu0(P->dp, nsys, fv, nullptr, lu, o.parilu_sweeps, ft, s);
+      e = launch_parilu0(P->dp, nsys, fv, nullptr, lu, o.parilu_sweeps, ft, s, o.parilu_res_tol,
+                         R ? R->parilu_sweeps : nullptr, R ? R->ilu_residual : nullptr,
+                         o.reduction == BILU_REDUCE_FAST ? 1 : 0);
     if (e != cudaSuccess) return cuda_fail(e, "factorisation");
     if (isai) {
       e = launch_isai(P->dp, nsys, lu, ws + off_ail, ws + off_aiu, fp32 ? 1 : 0, ft, s);

@@ -257,6 +257,7 @@ bilu_status upload(bilu_plan& P) {
                o_lur = put(P.lev_up_rows);
   const size_t o_dp = put(P.dep_ptr), o_dep = put(P.dep);
   const size_t o_lsrc = put(P.l_src), o_usrc = put(P.u_src);
+  const size_t o_rlev = put(P.row_lev), o_tpos = put(P.tpos), o_ment = put(P.mlp_ent);
   size_t o_alrp = 0, o_alci = 0, o_aurp = 0, o_auci = 0, o_alpp = 0, o_alp = 0, o_aupp = 0, o_aup = 0;
   if (P.has_isai) {
     o_alrp = put(P.ail_rp);
@@ -300,6 +301,10 @@ bilu_status upload(bilu_plan& P) {
   d.nnz_U = (int)P.u_src.size();
   d.l_src = b + o_lsrc;
   d.u_src = b + o_usrc;
+  d.row_lev = b + o_rlev;
+  d.tpos = b + o_tpos;
+  d.n_mlp = (int)P.mlp_ent.size();
+  d.mlp_ent = b + o_ment;
   if (P.has_isai) {
     d.ail_nnz = P.ail_rp[P.n];
     d.aiu_nnz = P.aiu_rp[P.n];
@@ -343,6 +348,7 @@ bilu_status check_opts(const bilu_options* o) {
     return set_error(BILU_ERR_INVALID, "options: reduction");
   if (o->threads_per_system < 0 || o->threads_per_system > 1024)
     return set_error(BILU_ERR_INVALID, "options: threads_per_system must be 0..1024");
+  if (!(o->parilu_res_tol >= 0.0)) return set_error(BILU_ERR_INVALID, "options: parilu_res_tol must be >= 0");
   return BILU_OK;
 }
 
@@ -368,6 +374,7 @@ void bilu_default_options(bilu_options* o) {
   o->reduction = BILU_REDUCE_REF;
   o->compute_true_residual = 1;
   o->threads_per_system = 0;
+  o->parilu_res_tol = 0.0;
 }
 
 const char* bilu_last_error(void) { return g_last_error.c_str(); }
@@ -470,6 +477,15 @@ bilu_status bilu_plan_create(bilu_plan** out, int n, int nnz, const int* h_rp, c
   }
   build_levels(*P);
   build_deps(*P);
+  P->row_lev.assign(n, 0);
+  for (int l = 0; l + 1 < (int)P->lev_lo_ptr.size(); ++l)
+    for (int q = P->lev_lo_ptr[l]; q < P->lev_lo_ptr[l + 1]; ++q) P->row_lev[P->lev_lo_rows[q]] = l;
+  P->tpos.assign(P->nnz, -1);
+  for (int i = 0; i < n; ++i)
+    for (int k = P->rp[i]; k < P->rp[i + 1]; ++k) {
+      P->tpos[k] = find_pos(P->rp, P->ci, P->ci[k], i);
+      if (P->ci[k] < i || P->dep_ptr[k + 1] > P->dep_ptr[k]) P->mlp_ent.push_back(k);
+    }
   P->has_isai = is_isai(P->opts.precond);
   if (P->has_isai) {
     st = build_isai(*P);
@@ -648,7 +664,9 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
     if (prec == BILU_PRECOND_ILU0_SPLIT || prec == BILU_PRECOND_ILU0_ISAI)
       e = launch_ilu0(P->dp, nsys, fv, lu, o.ilu_approach, ft, st);
     else
-      e = launch_parilu0(P->dp, nsys, fv, lu_init, lu, o.parilu_sweeps, ft, st);
+      e = launch_parilu0(P->dp, nsys, fv, lu_init, lu, o.parilu_sweeps, ft, st, o.parilu_res_tol,
+                         R ? R->parilu_sweeps : nullptr, R ? R->ilu_residual : nullptr,
+                         o.reduction == BILU_REDUCE_FAST ? 1 : 0);
     if (e != cudaSuccess) return cuda_err(e, "factorisation");
     if (is_isai(prec)) {
       void* ail = ws + off_ail;

@@ -86,24 +86,59 @@ __global__ void __launch_bounds__(512) k_ilu0(const DevPattern P, int nsys, cons
 // sweep t (parilu0_sweep_for_batch_entry_approach2's formula,
 // parILU_0_gpu.cu:18-57: sum of l_ik*u_kj by fma from 0 in ascending k, then
 // (a_ij - sum)/u_jj below the diagonal, (a_ij - sum)/1 elsewhere).
+// With res_tol > 0 the ILU residual of the current iterate,
+// ||(A - LU)|_S||_F / ||A||_F, is formed in the same pass (one more fma per
+// entry) and the sweeps stop once it is <= res_tol (at most `sweeps`).
+__device__ __forceinline__ double block_sum(double v, double* red) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(kFull, v, off);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+  return s;
+}
+
+// fast = true (BILU_REDUCE_FAST): the entries below the diagonal are
+// multiplied by reciprocals of the current diagonal, formed once per sweep,
+// instead of divided (n divisions per sweep instead of one per lower entry).
+template <bool FAST>
 __global__ void __launch_bounds__(512) k_parilu0(const DevPattern P, int nsys, const double* __restrict__ A,
                                                  const double* __restrict__ init, double* __restrict__ LUout,
-                                                 int sweeps) {
+                                                 int sweeps, double res_tol, int* __restrict__ sweeps_out,
+                                                 double* __restrict__ res_out) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double red[32];
   const int sys = blockIdx.x;
   if (sys >= nsys) return;
   const int nnz = P.nnz;
   double* As = reinterpret_cast<double*>(smem);
   double* cur = As + nnz;
   double* nxt = cur + nnz;
+  double* rinv = nxt + nnz;  // FAST only: n reciprocals
   const double* Ag = A + (size_t)sys * nnz;
   const double* Ig = init ? init + (size_t)sys * nnz : Ag;
+  double anorm2 = 0.0;
   for (int k = threadIdx.x; k < nnz; k += blockDim.x) {
-    As[k] = __ldg(Ag + k);
+    const double a = __ldg(Ag + k);
+    As[k] = a;
     cur[k] = __ldg(Ig + k);
+    anorm2 = fma(a, a, anorm2);
   }
+  const bool track = res_tol > 0.0 || res_out != nullptr;
+  if (track) anorm2 = block_sum(anorm2, red);
   __syncthreads();
-  for (int it = 0; it < sweeps; ++it) {
+  int done = 0;
+  double res = -1.0;
+  for (int it = 0; it <= sweeps; ++it) {
+    double r2 = 0.0;
+    const bool last = (it == sweeps);
+    if (last && !track) break;
+    if (FAST && !last) {
+      for (int r = threadIdx.x; r < P.n; r += blockDim.x) rinv[r] = 1.0 / cur[__ldg(P.diag + r)];
+      __syncthreads();
+    }
     for (int k = threadIdx.x; k < nnz; k += blockDim.x) {
       const int pb = __ldg(P.dep_ptr + k), pe = __ldg(P.dep_ptr + k + 1);
       double s = 0.0;
@@ -111,15 +146,34 @@ __global__ void __launch_bounds__(512) k_parilu0(const DevPattern P, int nsys, c
         const int2 d = __ldg(P.dep + q);
         s = fma(cur[d.x], cur[d.y], s);
       }
-      double v = As[k] - s;
       const int i = __ldg(P.row_of + k), j = __ldg(P.ci + k);
-      if (j < i) v = v / cur[__ldg(P.diag + j)];
-      nxt[k] = v;
+      if (track) {
+        const double lu = (j < i) ? fma(cur[k], cur[__ldg(P.diag + j)], s) : s + cur[k];
+        const double r = As[k] - lu;
+        r2 = fma(r, r, r2);
+      }
+      if (!last) {
+        double v = As[k] - s;
+        if (j < i) v = FAST ? v * rinv[j] : v / cur[__ldg(P.diag + j)];
+        nxt[k] = v;
+      }
     }
+    if (track) {
+      const double tot = block_sum(r2, red);
+      res = anorm2 > 0.0 ? sqrt(tot / anorm2) : sqrt(tot);
+      if (res_tol > 0.0 && res <= res_tol) break;  // uniform: every thread holds the same sum
+    }
+    if (last) break;
     __syncthreads();
     double* tswap = cur;
     cur = nxt;
     nxt = tswap;
+    ++done;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (sweeps_out) sweeps_out[sys] = done;
+    if (res_out) res_out[sys] = res;
   }
   for (int k = threadIdx.x; k < nnz; k += blockDim.x) LUout[(size_t)sys * nnz + k] = cur[k];
 }
@@ -268,12 +322,14 @@ cudaError_t launch_ilu0(const DevPattern& p, int nsys, const double* A, double* 
 }
 
 cudaError_t launch_parilu0(const DevPattern& p, int nsys, const double* A, const double* init, double* lu,
-                           int sweeps, int threads, cudaStream_t st) {
+                           int sweeps, int threads, cudaStream_t st, double res_tol, int* sweeps_out,
+                           double* res_out, int fast) {
   if (nsys == 0) return cudaSuccess;
-  const int smem = p.nnz * 8 * 3;
-  cudaError_t e = cudaFuncSetAttribute(k_parilu0, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  const int smem = p.nnz * 8 * 3 + (fast ? p.n * 8 : 0);
+  auto k = fast ? k_parilu0<true> : k_parilu0<false>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  k_parilu0<<<nsys, threads, smem, st>>>(p, nsys, A, init, lu, sweeps);
+  k<<<nsys, threads, smem, st>>>(p, nsys, A, init, lu, sweeps, res_tol, sweeps_out, res_out);
   return cudaGetLastError();
 }
 

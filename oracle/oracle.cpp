@@ -674,3 +674,150 @@ ORC_API void orc_set_num_threads(int t) {
   (void)t;
 #endif
 }
+
+// ===========================================================================
+// learned ParILU warm start (no reference counterpart): the library's
+// features (computed the same way, so bit-identical) and an FP64 forward /
+// backward of the 9-64-64-1 GELU network over BF16-rounded weights, for
+// checking the GPU training kernels.
+// ===========================================================================
+namespace {
+
+// round-to-nearest-even of an FP32 value to BF16 precision (IEEE rounding rule)
+inline float bf16_round(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;
+  u += 0x7fffu + ((u >> 16) & 1u);
+  u &= 0xffff0000u;
+  std::memcpy(&x, &u, 4);
+  return x;
+}
+
+constexpr int MF = 9, MH = 64;
+constexpr int MOW1 = 0, MOB1 = MH * MF, MOW2 = MOB1 + MH, MOB2 = MOW2 + MH * MH, MOW3 = MOB2 + MH, MOB3 = MOW3 + MH;
+constexpr int MNP = MOB3 + 1;
+
+// GELU, tanh form: 0.5 x (1 + tanh(k (x + c x^3))), k = sqrt(2/pi), c = 0.044715
+constexpr double kGk = 0.7978845608028654, kGc = 0.044715;
+inline double gelu_d(double x) { return 0.5 * x * (1.0 + std::tanh(kGk * (x + kGc * x * x * x))); }
+inline double gelu_dd(double x) {
+  const double t = std::tanh(kGk * (x + kGc * x * x * x));
+  return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * kGk * (1.0 + 3.0 * kGc * x * x);
+}
+
+}  // namespace
+
+ORC_API int orc_mlp_param_count(void) { return MNP; }
+
+// features of entries idx[q] = s*nnz + e (factor pattern with every diagonal)
+ORC_API void orc_mlp_features(int n, int nnz, const int* rp, const int* ci, int nsys, const double* vals, int nsample,
+                              const int* idx, float* feat, double* base) {
+  std::vector<int> diag(n), rowof(nnz), tpos(nnz, -1), lev(n, 0);
+  orc_find_diag(n, rp, ci, diag.data());
+  int nlev = 0;
+  for (int i = 0; i < n; ++i) {
+    int l = 0;
+    for (int k = rp[i]; k < diag[i]; ++k) l = std::max(l, lev[ci[k]] + 1);
+    lev[i] = l;
+    nlev = std::max(nlev, l + 1);
+    for (int k = rp[i]; k < rp[i + 1]; ++k) {
+      rowof[k] = i;
+      const int j = ci[k];
+      for (int t = rp[j]; t < rp[j + 1]; ++t)
+        if (ci[t] == i) tpos[k] = t;
+    }
+  }
+  for (int q = 0; q < nsample; ++q) {
+    const long long g = idx[q];
+    const int s = (int)(g / nnz), e = (int)(g % nnz);
+    const double* As = vals + (size_t)s * nnz;
+    auto stats = [&](int r, float& rn, float& cn, float& cr) {
+      double a = 0.0, b = 0.0, c = 0.0;
+      for (int k = rp[r]; k < rp[r + 1]; ++k) {
+        a = std::fma(As[k], As[k], a);
+        const int t = tpos[k];
+        if (t >= 0) {
+          b = std::fma(As[t], As[t], b);
+          if (k < diag[r]) c = std::fma(As[k], As[t] / As[diag[ci[k]]], c);
+        }
+      }
+      rn = (float)std::sqrt(a);
+      cn = (float)std::sqrt(b);
+      cr = (float)c;
+    };
+    const int i = rowof[e], j = ci[e];
+    float rni, cni, cri, rnj, cnj, crj;
+    stats(i, rni, cni, cri);
+    stats(j, rnj, cnj, crj);
+    const float fij = (float)As[e], fii = (float)As[diag[i]], fjj = (float)As[diag[j]];
+    const float inv = 1.0f / (fii != 0.0f ? std::fabs(fii) : 1.0f);
+    float* f = feat + (size_t)q * MF;
+    f[0] = fij * inv;
+    f[1] = fii * inv;
+    f[2] = fjj * inv;
+    f[3] = rni * inv;
+    f[4] = cnj * inv;
+    f[5] = nlev > 1 ? (float)lev[i] / (float)(nlev - 1) : 0.0f;
+    f[6] = j < i ? -1.0f : (j > i ? 1.0f : 0.0f);
+    f[7] = cri * inv;
+    f[8] = crj * inv;
+    float bs = 1.0f;
+    if (j < i) {
+      const float den = fjj - crj;
+      bs = den != 0.0f ? 1.0f / den : (fjj != 0.0f ? 1.0f / fjj : 1.0f);
+    } else if (j == i) {
+      bs = fii != 0.0f ? (fii - cri) / fii : 1.0f;
+    }
+    base[q] = (double)bs;
+  }
+}
+
+// mean squared error over the samples and its gradient (FP64 arithmetic,
+// weights rounded to BF16 as the GPU computes with them); returns the loss;
+// out (optional) receives the network outputs
+ORC_API double orc_mlp_loss_grad(const float* params, int nsample, const float* feat, const float* y, double* grad,
+                                 double* out) {
+  std::vector<double> w(MNP);
+  for (int k = 0; k < MNP; ++k) w[k] = (double)bf16_round(params[k]);
+  std::fill(grad, grad + MNP, 0.0);
+  double loss = 0.0;
+  for (int q = 0; q < nsample; ++q) {
+    const float* x = feat + (size_t)q * MF;
+    double p1[MH], h1[MH], p2[MH], h2[MH];
+    for (int u = 0; u < MH; ++u) {
+      double a = w[MOB1 + u];
+      for (int k = 0; k < MF; ++k) a += w[MOW1 + u * MF + k] * (double)x[k];
+      p1[u] = a;
+      h1[u] = gelu_d(a);
+    }
+    double o = w[MOB3];
+    for (int u = 0; u < MH; ++u) {
+      double a = w[MOB2 + u];
+      for (int v = 0; v < MH; ++v) a += w[MOW2 + u * MH + v] * h1[v];
+      p2[u] = a;
+      h2[u] = gelu_d(a);
+      o += w[MOW3 + u] * h2[u];
+    }
+    if (out) out[q] = o;
+    const double diff = o - (double)y[q];
+    loss += diff * diff / nsample;
+    const double dout = 2.0 * diff / nsample;
+    grad[MOB3] += dout;
+    double dp2[MH];
+    for (int u = 0; u < MH; ++u) {
+      grad[MOW3 + u] += dout * h2[u];
+      dp2[u] = dout * w[MOW3 + u] * gelu_dd(p2[u]);
+      grad[MOB2 + u] += dp2[u];
+      for (int v = 0; v < MH; ++v) grad[MOW2 + u * MH + v] += dp2[u] * h1[v];
+    }
+    for (int v = 0; v < MH; ++v) {
+      double dh = 0.0;
+      for (int u = 0; u < MH; ++u) dh += w[MOW2 + u * MH + v] * dp2[u];
+      const double dp1 = dh * gelu_dd(p1[v]);
+      grad[MOB1 + v] += dp1;
+      for (int k = 0; k < MF; ++k) grad[MOW1 + v * MF + k] += dp1 * (double)x[k];
+    }
+  }
+  return loss;
+}

@@ -211,3 +211,26 @@ def dense_solve(rp, ci, A, b, sys_ids=None):
     out = np.zeros((m, b.shape[1]))
     lib().orc_dense_solve(b.shape[1], A.shape[1], _i(rp), _i(ci), m, _i(ids), _d(A), _d(b), _d(out))
     return out
+
+
+# ---------------------------------------------------------------- learned warm start
+def mlp_features(rp, ci, vals, idx):
+    rp, ci = _ia(rp), _ia(ci)
+    vals = np.ascontiguousarray(vals, np.float64)
+    idx = _ia(idx)
+    feat = np.zeros((len(idx), 9), np.float32)
+    base = np.zeros(len(idx))
+    lib().orc_mlp_features(len(rp) - 1, vals.shape[1], _i(rp), _i(ci), vals.shape[0], _d(vals), len(idx), _i(idx),
+                           _f(feat), _d(base))
+    return feat, base
+
+
+def mlp_loss_grad(params, feat, y):
+    lib().orc_mlp_loss_grad.restype = C.c_double
+    params = np.ascontiguousarray(params, np.float32)
+    feat = np.ascontiguousarray(feat, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    grad = np.zeros(len(params))
+    out = np.zeros(len(y))
+    loss = lib().orc_mlp_loss_grad(_f(params), len(y), _f(feat), _f(y), _d(grad), _d(out))
+    return loss, grad, out
