@@ -65,6 +65,9 @@ typedef int bilu_status;
 #define BILU_PRECOND_PARILU0_ISAI 4  /* ParILU(0) then ISAI of L and U
                                         [Batched_ILU_ISAI_Preconditioned_BiCGSTAB_Gpu, is_parilu = 1]      */
 #define BILU_PRECOND_NONE         5  /* unpreconditioned BiCGSTAB (identity preconditioner)               */
+#define BILU_PRECOND_GENERAL_ISAI 6  /* ISAI of A itself (pattern of |A|^isai_power, Gauss-Jordan row solves
+                                        with partial pivoting), applied as one SpMV
+                                        [Batched_General_ISAI_Preconditioned_BiCGSTAB_Gpu, power 1]       */
 
 #define BILU_TOL_ABS   0  /* stop when ||r||_2 < tol            (reference: ATOL = 1e-11, PrecondBiCGSTAB.h:12) */
 #define BILU_TOL_REL   1  /* stop when ||r||_2 < tol * ||b||_2                                                   */
@@ -226,6 +229,9 @@ bilu_status bilu_split_lu(const bilu_plan* plan, int nsys, const double* d_lu,
 
 /* ISAI of L and U from in-place factors d_lu: d_ail (nsys*nnz_isai_L),
  * d_aiu (nsys*nnz_isai_U) on the plan's ISAI patterns (pattern of |T|^power).
+ * For a BILU_PRECOND_GENERAL_ISAI plan: d_lu holds A's values (factor pattern),
+ * d_ail receives the ISAI of A (GenerateISAI_gpu(aiA, A, general, p)) and
+ * d_aiu is not used.
  * Replaces GenerateISAI_gpu(aiL, L, lower_tri, p) and (aiU, U, upper_tri, p)
  * (isai.h:9, isai_gpu.cu:720). */
 bilu_status bilu_isai(const bilu_plan* plan, int nsys, const double* d_lu,

@@ -20,7 +20,8 @@ ERR_INVALID, ERR_PATTERN, ERR_CAPACITY, ERR_CUDA, ERR_NO_DEVICE, ERR_ALLOC = 1, 
 
 SYS_CONVERGED, SYS_MAX_ITER, SYS_BREAKDOWN_RHO, SYS_NONFINITE, SYS_ZERO_RHS, SYS_INITIAL_OK = 1, -1, -2, -3, 2, 3
 
-PRECOND_ILU0, PRECOND_ILU0_SPLIT, PRECOND_PARILU0, PRECOND_ILU0_ISAI, PRECOND_PARILU0_ISAI, PRECOND_NONE = range(6)
+(PRECOND_ILU0, PRECOND_ILU0_SPLIT, PRECOND_PARILU0, PRECOND_ILU0_ISAI, PRECOND_PARILU0_ISAI, PRECOND_NONE,
+ PRECOND_GENERAL_ISAI) = range(7)
 TOL_ABS, TOL_REL = 0, 1
 FP64, FP32 = 0, 1
 REDUCE_REF, REDUCE_FAST = 0, 1

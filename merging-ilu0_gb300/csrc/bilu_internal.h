@@ -61,6 +61,12 @@ struct DevPattern {
   const int2* ail_prog = nullptr;
   const int* aiu_prog_ptr = nullptr;
   const int2* aiu_prog = nullptr;
+  // general ISAI: per row the sz*sz positions of A(J_k, J_t) in the factor
+  // pattern (row-major over k, -1 = structural zero), and the position of i in J
+  int gen_maxs = 0;
+  const int* gen_map_ptr = nullptr;  // n+1
+  const int* gen_map = nullptr;
+  const int* gen_pos = nullptr;      // n
   // input -> factor pattern value map (src index or -1 for inserted diagonals)
   int nnz_in = 0;
   const int* src_map = nullptr;  // nnz
@@ -209,6 +215,8 @@ cudaError_t launch_mlp_warm(const DevPattern& p, int nsys, const double* A, cons
                             const float* corr, const void* pbf, double threshold, double* lu0, double* res, int* used,
                             cudaStream_t st);
 cudaError_t launch_to_float(const double* a, float* b, size_t n, cudaStream_t st);
+cudaError_t launch_isai_general(const DevPattern& p, int nsys, const double* A, void* ai, int fp32, int threads,
+                                cudaStream_t st);
 cudaError_t launch_split(const DevPattern& p, int nsys, const double* lu, double* L, double* U, cudaStream_t st);
 cudaError_t launch_true_residual(const DevPattern& p, int nsys, const double* A, const double* b, const double* x,
                                  double* out, int threads, cudaStream_t st);
@@ -231,6 +239,8 @@ struct bilu_plan {
   bool has_isai = false;
   std::vector<int> ail_rp, ail_ci, aiu_rp, aiu_ci;
   std::vector<int> ail_prog_ptr, ail_prog, aiu_prog_ptr, aiu_prog;  // prog in int units (pairs)
+  bool general_isai = false;
+  std::vector<int> gen_map_ptr, gen_map, gen_pos;
   int* dbuf = nullptr;
   bilu::DevPattern dp;
   // solver kernel configuration

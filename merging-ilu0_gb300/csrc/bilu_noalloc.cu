@@ -85,7 +85,8 @@ extern "C" bilu_status bilu_solve_noalloc(bilu_plan* P, int nsys, const double* 
   const bilu_options& o = P->opts;
   const int prec = o.precond;
   const bool fp32 = o.factor_precision == BILU_FP32;
-  const bool isai = prec == BILU_PRECOND_ILU0_ISAI || prec == BILU_PRECOND_PARILU0_ISAI;
+  const bool isai =
+      prec == BILU_PRECOND_ILU0_ISAI || prec == BILU_PRECOND_PARILU0_ISAI || prec == BILU_PRECOND_GENERAL_ISAI;
   const bool needs_factors = !(prec == BILU_PRECOND_ILU0 || prec == BILU_PRECOND_NONE);
   // scratch layout: [expanded values][LU][LU as float | aiL][aiU]
   const size_t nz = (size_t)P->nnz * nsys;
@@ -145,7 +146,10 @@ extern "C" bilu_status bilu_solve_noalloc(bilu_plan* P, int nsys, const double* 
       fv = reinterpret_cast<const double*>(ws + off_exp);
     }
     double* lu = reinterpret_cast<double*>(ws + off_lu);
-    if (prec == BILU_PRECOND_ILU0_SPLIT || prec == BILU_PRECOND_ILU0_ISAI)
+    if (prec == BILU_PRECOND_GENERAL_ISAI) {
+      e = launch_isai_general(P->dp, nsys, fv, ws + off_ail, fp32 ? 1 : 0, ft, s);
+      if (e != cudaSuccess) return cuda_fail(e, "general isai");
+    } else if (prec == BILU_PRECOND_ILU0_SPLIT || prec == BILU_PRECOND_ILU0_ISAI)
       e = launch_ilu0(P->dp, nsys, fv, lu, o.ilu_approach, ft, s);
     else
       e = launch_parilu0(P->dp, nsys, fv, nullptr, lu, o.parilu_sweeps, ft, s, o.parilu_res_tol,
@@ -153,11 +157,13 @@ extern "C" bilu_status bilu_solve_noalloc(bilu_plan* P, int nsys, const double* 
                          o.reduction == BILU_REDUCE_FAST ? 1 : 0);
     if (e != cudaSuccess) return cuda_fail(e, "factorisation");
     if (isai) {
-      e = launch_isai(P->dp, nsys, lu, ws + off_ail, ws + off_aiu, fp32 ? 1 : 0, ft, s);
-      if (e != cudaSuccess) return cuda_fail(e, "isai");
+      if (prec != BILU_PRECOND_GENERAL_ISAI) {
+        e = launch_isai(P->dp, nsys, lu, ws + off_ail, ws + off_aiu, fp32 ? 1 : 0, ft, s);
+        if (e != cudaSuccess) return cuda_fail(e, "isai");
+      }
       a.prec = PK_ISAI;
       a.ail = ws + off_ail;
-      a.aiu = ws + off_aiu;
+      a.aiu = prec == BILU_PRECOND_GENERAL_ISAI ? nullptr : ws + off_aiu;
     } else {
       a.prec = PK_LU_GLOBAL;
       if (fp32) {

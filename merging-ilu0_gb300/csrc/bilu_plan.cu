@@ -105,7 +105,9 @@ using namespace bilu;
 namespace plan_detail {
 
 bool is_fp32(const bilu_options& o) { return o.factor_precision == BILU_FP32; }
-bool is_isai(int p) { return p == BILU_PRECOND_ILU0_ISAI || p == BILU_PRECOND_PARILU0_ISAI; }
+bool is_isai(int p) {
+  return p == BILU_PRECOND_ILU0_ISAI || p == BILU_PRECOND_PARILU0_ISAI || p == BILU_PRECOND_GENERAL_ISAI;
+}
 
 int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
@@ -161,7 +163,35 @@ void pattern_power(int n, const std::vector<int>& trp, const std::vector<int>& t
   oci.swap(cci);
 }
 
+// general ISAI of A: pattern of |A|^power, per-row position maps of A(J,J)
+bilu_status build_isai_general(bilu_plan& P) {
+  const int n = P.n;
+  const int power = std::max(1, P.opts.isai_power);
+  pattern_power(n, P.rp, P.ci, power, P.ail_rp, P.ail_ci);
+  P.aiu_rp.assign(n + 1, 0);
+  P.aiu_ci.clear();
+  P.ail_prog_ptr.assign(n + 1, 0);
+  P.aiu_prog_ptr.assign(n + 1, 0);
+  P.gen_map_ptr.assign(n + 1, 0);
+  P.gen_map.clear();
+  P.gen_pos.assign(n, 0);
+  for (int i = 0; i < n; ++i) {
+    const int beg = P.ail_rp[i], sz = P.ail_rp[i + 1] - beg;
+    if (sz > 32)
+      return set_error(BILU_ERR_CAPACITY, "general ISAI row " + std::to_string(i) + " has " + std::to_string(sz) +
+                                              " entries (limit 32, isai_gpu.cu:223)");
+    const int* J = P.ail_ci.data() + beg;
+    for (int t = 0; t < sz; ++t)
+      if (J[t] == i) P.gen_pos[i] = t;
+    for (int k = 0; k < sz; ++k)
+      for (int t = 0; t < sz; ++t) P.gen_map.push_back(find_pos(P.rp, P.ci, J[k], J[t]));
+    P.gen_map_ptr[i + 1] = (int)P.gen_map.size();
+  }
+  return BILU_OK;
+}
+
 bilu_status build_isai(bilu_plan& P) {
+  if (P.general_isai) return build_isai_general(P);
   const int n = P.n;
   const int power = std::max(1, P.opts.isai_power);
   pattern_power(n, P.l_rp, P.l_ci, power, P.ail_rp, P.ail_ci);
@@ -227,7 +257,8 @@ int prec_kind(int precond) {
     case BILU_PRECOND_ILU0_SPLIT:
     case BILU_PRECOND_PARILU0: return PK_LU_GLOBAL;
     case BILU_PRECOND_ILU0_ISAI:
-    case BILU_PRECOND_PARILU0_ISAI: return PK_ISAI;
+    case BILU_PRECOND_PARILU0_ISAI:
+    case BILU_PRECOND_GENERAL_ISAI: return PK_ISAI;
     default: return PK_NONE;
   }
 }
@@ -259,6 +290,12 @@ bilu_status upload(bilu_plan& P) {
   const size_t o_lsrc = put(P.l_src), o_usrc = put(P.u_src);
   const size_t o_rlev = put(P.row_lev), o_tpos = put(P.tpos), o_ment = put(P.mlp_ent);
   size_t o_alrp = 0, o_alci = 0, o_aurp = 0, o_auci = 0, o_alpp = 0, o_alp = 0, o_aupp = 0, o_aup = 0;
+  size_t o_gmp = 0, o_gm = 0, o_gp = 0;
+  if (P.general_isai) {
+    o_gmp = put(P.gen_map_ptr);
+    o_gm = put(P.gen_map);
+    o_gp = put(P.gen_pos);
+  }
   if (P.has_isai) {
     o_alrp = put(P.ail_rp);
     o_alci = put(P.ail_ci);
@@ -317,6 +354,12 @@ bilu_status upload(bilu_plan& P) {
     d.aiu_prog_ptr = b + o_aupp;
     d.aiu_prog = reinterpret_cast<const int2*>(b + o_aup);
   }
+  if (P.general_isai) {
+    d.gen_map_ptr = b + o_gmp;
+    d.gen_map = b + o_gm;
+    d.gen_pos = b + o_gp;
+    for (int i = 0; i < P.n; ++i) d.gen_maxs = std::max(d.gen_maxs, P.ail_rp[i + 1] - P.ail_rp[i]);
+  }
   return BILU_OK;
 }
 
@@ -335,7 +378,7 @@ size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
 
 bilu_status check_opts(const bilu_options* o) {
   if (!o) return BILU_OK;
-  if (o->precond < 0 || o->precond > BILU_PRECOND_NONE) return set_error(BILU_ERR_INVALID, "options: bad precond");
+  if (o->precond < 0 || o->precond > BILU_PRECOND_GENERAL_ISAI) return set_error(BILU_ERR_INVALID, "options: bad precond");
   if (o->ilu_approach < 1 || o->ilu_approach > 4) return set_error(BILU_ERR_INVALID, "options: ilu_approach must be 1..4");
   if (o->parilu_sweeps < 0) return set_error(BILU_ERR_INVALID, "options: parilu_sweeps < 0");
   if (o->isai_power < 1) return set_error(BILU_ERR_INVALID, "options: isai_power < 1");
@@ -487,6 +530,7 @@ bilu_status bilu_plan_create(bilu_plan** out, int n, int nnz, const int* h_rp, c
       if (P->ci[k] < i || P->dep_ptr[k + 1] > P->dep_ptr[k]) P->mlp_ent.push_back(k);
     }
   P->has_isai = is_isai(P->opts.precond);
+  P->general_isai = P->opts.precond == BILU_PRECOND_GENERAL_ISAI;
   if (P->has_isai) {
     st = build_isai(*P);
     if (st) {
@@ -661,6 +705,13 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
     const double* fv = factor_values(P, nsys, vals, (double*)(ws + off_exp), st, &e);
     if (e != cudaSuccess) return cuda_err(e, "expand");
     double* lu = (double*)(ws + off_lu);
+    if (prec == BILU_PRECOND_GENERAL_ISAI) {
+      e = launch_isai_general(P->dp, nsys, fv, ws + off_ail, fp32 ? 1 : 0, ft, st);
+      if (e != cudaSuccess) return cuda_err(e, "general isai");
+      a.prec = PK_ISAI;
+      a.ail = ws + off_ail;
+      a.aiu = nullptr;
+    } else {
     if (prec == BILU_PRECOND_ILU0_SPLIT || prec == BILU_PRECOND_ILU0_ISAI)
       e = launch_ilu0(P->dp, nsys, fv, lu, o.ilu_approach, ft, st);
     else
@@ -686,6 +737,7 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
       } else {
         a.F = lu;
       }
+    }
     }
   }
   int maxl = P->a_maxl;
@@ -764,9 +816,12 @@ bilu_status bilu_split_lu(const bilu_plan* P, int nsys, const double* d_lu, doub
 }
 
 bilu_status bilu_isai(const bilu_plan* P, int nsys, const double* d_lu, double* d_ail, double* d_aiu, void* stream) {
-  if (!P || nsys < 0 || (nsys > 0 && (!d_lu || !d_ail || !d_aiu))) return set_error(BILU_ERR_INVALID, "bilu_isai: bad args");
+  if (!P || nsys < 0 || (nsys > 0 && (!d_lu || !d_ail || (!d_aiu && !P->general_isai))))
+    return set_error(BILU_ERR_INVALID, "bilu_isai: bad args");
   if (!P->has_isai) return set_error(BILU_ERR_INVALID, "bilu_isai: plan was not created with an ISAI preconditioner");
-  cudaError_t e = launch_isai(P->dp, nsys, d_lu, d_ail, d_aiu, 0, fact_threads(P), (cudaStream_t)stream);
+  cudaError_t e = P->general_isai
+                      ? launch_isai_general(P->dp, nsys, d_lu, d_ail, 0, fact_threads(P), (cudaStream_t)stream)
+                      : launch_isai(P->dp, nsys, d_lu, d_ail, d_aiu, 0, fact_threads(P), (cudaStream_t)stream);
   return e == cudaSuccess ? BILU_OK : cuda_err(e, "isai");
 }
 

@@ -240,6 +240,65 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
   for (int k = threadIdx.x; k < P.aiu_nnz; k += blockDim.x) aiu[(size_t)sys * P.aiu_nnz + k] = (FT)M[k];
 }
 
+// ---------------------------------------------------------------- general ISAI
+// ISAI of A itself (solve_general_dense, isai_gpu.cu:392-554), one thread per
+// ISAI row and system.  Lane t of the reference holds row t of A(J,J)^T; here
+// T[t][k] = A(J_k, J_t) and the thread runs every lane's operations in the
+// same order: for each pivot column dp, the pivot is the first row with the
+// largest |T[r][dp]| (the reference's shfl_down tree keeps the lower lane on
+// ties), rows are swapped with the right-hand side, every other row r does
+// T[r][c] = fma(-m_r, T[dp][c], T[r][c]) with m_r = T[r][dp] / T[dp][dp], and
+// finally sol_t / T[t][t].
+template <typename FT, int MAXS>
+__global__ void __launch_bounds__(256) k_isai_general(const DevPattern P, int nsys, const double* __restrict__ A,
+                                                      FT* __restrict__ ai) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sys = blockIdx.x;
+  if (sys >= nsys) return;
+  double* As = reinterpret_cast<double*>(smem);
+  for (int k = threadIdx.x; k < P.nnz; k += blockDim.x) As[k] = __ldg(A + (size_t)sys * P.nnz + k);
+  __syncthreads();
+  for (int i = threadIdx.x; i < P.n; i += blockDim.x) {
+    const int beg = __ldg(P.ail_rp + i), sz = __ldg(P.ail_rp + i + 1) - beg;
+    const int* map = P.gen_map + __ldg(P.gen_map_ptr + i);
+    double T[MAXS][MAXS], sol[MAXS];
+    for (int k = 0; k < sz; ++k)
+      for (int t = 0; t < sz; ++t) {
+        const int pos = __ldg(map + k * sz + t);
+        T[t][k] = pos >= 0 ? As[pos] : 0.0;
+      }
+    const int pi = __ldg(P.gen_pos + i);
+    for (int t = 0; t < sz; ++t) sol[t] = (t == pi) ? 1.0 : 0.0;
+    for (int dp = 0; dp < sz; ++dp) {
+      int piv = dp;
+      double best = fabs(T[dp][dp]);
+      for (int r = dp + 1; r < sz; ++r)
+        if (fabs(T[r][dp]) > best) {
+          best = fabs(T[r][dp]);
+          piv = r;
+        }
+      if (piv != dp) {
+        for (int c = 0; c < sz; ++c) {
+          const double tmp = T[dp][c];
+          T[dp][c] = T[piv][c];
+          T[piv][c] = tmp;
+        }
+        const double tmp = sol[dp];
+        sol[dp] = sol[piv];
+        sol[piv] = tmp;
+      }
+      const double d = T[dp][dp];
+      for (int r = 0; r < sz; ++r) {
+        if (r == dp) continue;
+        const double mult = T[r][dp] / d;
+        for (int c = 0; c < sz; ++c) T[r][c] = fma(-mult, T[dp][c], T[r][c]);
+        sol[r] = fma(-mult, sol[dp], sol[r]);
+      }
+    }
+    for (int t = 0; t < sz; ++t) ai[(size_t)sys * P.ail_nnz + beg + t] = (FT)(sol[t] / T[t][t]);
+  }
+}
+
 // ---------------------------------------------------------------- L / U split
 __global__ void k_split(const DevPattern P, int nsys, const double* __restrict__ LU, double* __restrict__ L,
                         double* __restrict__ U) {
@@ -354,6 +413,24 @@ cudaError_t launch_to_float(const double* a, float* b, size_t n, cudaStream_t st
   if (n == 0) return cudaSuccess;
   k_to_float<<<grid_for(n, 256), 256, 0, st>>>(a, b, n);
   return cudaGetLastError();
+}
+
+cudaError_t launch_isai_general(const DevPattern& p, int nsys, const double* A, void* ai, int fp32, int threads,
+                                cudaStream_t st) {
+  if (nsys == 0) return cudaSuccess;
+  const int smem = p.nnz * 8;
+  threads = threads > 256 ? 256 : threads;
+  void* k;
+  if (p.gen_maxs <= 8)
+    k = fp32 ? (void*)k_isai_general<float, 8> : (void*)k_isai_general<double, 8>;
+  else if (p.gen_maxs <= 16)
+    k = fp32 ? (void*)k_isai_general<float, 16> : (void*)k_isai_general<double, 16>;
+  else
+    k = fp32 ? (void*)k_isai_general<float, 32> : (void*)k_isai_general<double, 32>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {const_cast<DevPattern*>(&p), &nsys, &A, &ai};
+  return cudaLaunchKernel(k, dim3(nsys), dim3(threads), args, (size_t)smem, st);
 }
 
 cudaError_t launch_split(const DevPattern& p, int nsys, const double* lu, double* L, double* U, cudaStream_t st) {

@@ -386,6 +386,17 @@ __device__ __forceinline__ void solve_one(const SolveArgs& a, const DevPattern& 
         trsv_f64<REF>(P, reinterpret_cast<const double*>(F), reinterpret_cast<const double*>(rinv_raw), in, out,
                       team);
       }
+    } else if (a.prec == PK_ISAI && P.aiu_nnz == 0) {  // general ISAI: z = aiA * v
+      if (kFP32) {
+        float* fin = fy;
+        for (int i = tid; i < n; i += nt) fin[i] = (float)in[i];
+        __syncthreads();
+        const float* L = reinterpret_cast<const float*>(AIL);
+        for (int i = tid; i < n; i += nt)
+          out[i] = (double)row_f32(L, P.ail_ci, __ldg(P.ail_rp + i), __ldg(P.ail_rp + i + 1), fin);
+      } else {
+        spmv<REF, S>(n, P.ail_rp, P.ail_ci, reinterpret_cast<const double*>(AIL), in, out);
+      }
     } else if (a.prec == PK_ISAI) {
       if (kFP32) {
         float* fin = fy;

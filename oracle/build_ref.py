@@ -36,6 +36,7 @@ UNITS = [
     ("ilu0", "ILU_0_gpu.cu"),
     ("parilu", "parILU_0_gpu.cu"),
     ("isai", "isai_gpu.cu"),
+    ("general_isai", "PrecondBiCGSTAB_general_isai_gpu.cu"),
 ]
 MAX_NUM_ROWS = 512
 MAX_NUM_NZ = 2560

@@ -416,6 +416,7 @@ ORC_API int orc_isai_pattern(int n, const int* rp, const int* ci, int power, con
 //   upper T (tri = 1): forward substitution, rhs e_0 (solve_lower_tri_dense):
 //     for col = 0 .. |J|-1, lanes t > col update.
 // Missing entries of T(J,J) are zeros (they give exact zero updates).
+//   general T (tri = 2): Gauss-Jordan with partial pivoting, rhs e_pos(i).
 // T is given in the reference's separate CSR form (t_rp/t_ci/t_vals; for L
 // the explicit unit diagonal is part of the pattern).
 ORC_API int orc_isai_values(int n, const int* t_rp, const int* t_ci, int t_nnz, int nsys, const double* t_vals,
@@ -445,13 +446,44 @@ ORC_API int orc_isai_values(int n, const int* t_rp, const int* t_ci, int t_nnz, 
           const double bot = sol[col];
           for (int t = 0; t < col; ++t) sol[t] = std::fma(-bot, loc[t][col], sol[t]);
         }
-      } else {
+      } else if (tri == 1) {
         for (int t = 0; t < sz; ++t) sol[t] = (t == 0) ? 1.0 : 0.0;
         for (int col = 0; col < sz; ++col) {
           sol[col] = sol[col] / loc[col][col];
           const double top = sol[col];
           for (int t = col + 1; t < sz; ++t) sol[t] = std::fma(-top, loc[t][col], sol[t]);
         }
+      } else {
+        // general (solve_general_dense, isai_gpu.cu:392-554): Gauss-Jordan on the
+        // rows of T(J,J)^T (one lane each in the reference) with partial pivoting.
+        // choose_pivot_row_1's shfl_down tree with strict > keeps the lower lane on
+        // ties, and lanes outside [dp, sz) carry row dp's value: the pivot is the
+        // first row with the largest |a_r[dp]|.
+        int pos = 0;
+        for (int t = 0; t < sz; ++t)
+          if (J[t] == i) pos = t;
+        for (int t = 0; t < sz; ++t) sol[t] = (t == pos) ? 1.0 : 0.0;
+        for (int dp = 0; dp < sz; ++dp) {
+          int piv = dp;
+          double best = std::fabs(loc[dp][dp]);
+          for (int r = dp + 1; r < sz; ++r)
+            if (std::fabs(loc[r][dp]) > best) {
+              best = std::fabs(loc[r][dp]);
+              piv = r;
+            }
+          if (piv != dp) {
+            for (int c = 0; c < sz; ++c) std::swap(loc[dp][c], loc[piv][c]);
+            std::swap(sol[dp], sol[piv]);
+          }
+          const double d = loc[dp][dp];
+          for (int r = 0; r < sz; ++r) {
+            if (r == dp) continue;
+            const double mult = loc[r][dp] / d;
+            for (int c = 0; c < sz; ++c) loc[r][c] = std::fma(-mult, loc[dp][c], loc[r][c]);
+            sol[r] = std::fma(-mult, sol[dp], sol[r]);
+          }
+        }
+        for (int t = 0; t < sz; ++t) sol[t] = sol[t] / loc[t][t];
       }
       for (int t = 0; t < sz; ++t) M[beg + t] = sol[t];
     }
@@ -471,7 +503,9 @@ ORC_API int orc_isai_values(int n, const int* t_rp, const int* t_ci, int t_nnz, 
 //       1 = ISAI: z = aiU * (aiL * v), both with the SpMV tree order;
 //       2 = identity;
 //       3 = in-place LU stored as float (lu_f32), applied in FP32 (library mode);
-//       4 = ISAI stored as float (ail_f/aiu_f), applied in FP32.
+//       4 = ISAI stored as float (ail_f/aiu_f), applied in FP32;
+//       5 = general ISAI of A: z = aiA * v (PrecondBiCGSTAB_general_isai_gpu.cu:23-30);
+//       6 = the same stored and applied in FP32.
 // dot: 0 = warp-0 tree inner products (ILU solver kernels),
 //      1 = serial inner products (ISAI solver kernel).
 // tol_mode: 0 = absolute (||r|| < tol, the reference's ATOL), 1 = relative to ||b||.
@@ -517,6 +551,12 @@ ORC_API void orc_bicgstab(int n, int nnz, const int* rp, const int* ci, int nsys
         spmv_tree(n, aiu_rp, aiu_ci, AIU, tmp.data(), out);
       } else if (prec == 3) {
         trsv_lu_f32(n, f_rp, f_ci, diag.data(), LUf, rinvf.data(), in, yf.data(), out);
+      } else if (prec == 5) {
+        spmv_tree(n, ail_rp, ail_ci, AIL, in, out);
+      } else if (prec == 6) {
+        for (int i = 0; i < n; ++i) fin[i] = (float)in[i];
+        spmv_f32(n, ail_rp, ail_ci, AILf, fin.data(), fmid.data());
+        for (int i = 0; i < n; ++i) out[i] = (double)fmid[i];
       } else if (prec == 4) {
         for (int i = 0; i < n; ++i) fin[i] = (float)in[i];
         spmv_f32(n, ail_rp, ail_ci, AILf, fin.data(), fmid.data());

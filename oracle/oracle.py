@@ -157,7 +157,7 @@ def isai_values(trp, tci, tvals, tri, arp, aci):
     return out
 
 
-PREC_LU, PREC_ISAI, PREC_NONE, PREC_LU_F32, PREC_ISAI_F32 = 0, 1, 2, 3, 4
+PREC_LU, PREC_ISAI, PREC_NONE, PREC_LU_F32, PREC_ISAI_F32, PREC_GISAI, PREC_GISAI_F32 = 0, 1, 2, 3, 4, 5, 6
 
 
 def bicgstab(rp, ci, A, b, prec=PREC_LU, lu=None, ail=None, aiu=None, dot=0, tol_mode=0, tol=1e-11, max_iter=500,

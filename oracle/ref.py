@@ -28,7 +28,7 @@ _lib = None
 def available():
     return os.path.exists(LIBPATH) and all(
         os.path.exists(os.path.join(REFDIR, u + ".cubin"))
-        for u in ("merged", "ilu_split", "ilu_isai", "ilu0", "parilu", "isai"))
+        for u in ("merged", "ilu_split", "ilu_isai", "ilu0", "parilu", "isai", "general_isai"))
 
 
 def lib(device=0):
@@ -243,3 +243,18 @@ def isai_solve(dev, rp, ci, vals, b, ail, aiu):
           len(ail[1]), T(ail[0], torch.int32), T(ail[1], torch.int32), T(ail[2]), len(aiu[1]),
           T(aiu[0], torch.int32), T(aiu[1], torch.int32), T(aiu[2]), it, cv, rs)
     return {"x": X.cpu().numpy(), "iters": it.cpu().numpy(), "conv": cv.cpu().numpy(), "res": rs.cpu().numpy()}
+
+
+def general_isai_solve(dev, rp, ci, vals, b, ai):
+    """KernelBatchedPreconditionedBiCGSTABGeneralISAI with (row_ptrs, col_idxs, values) of aiA."""
+    import torch
+    nsys, n = b.shape
+    T = lambda a, dt=None: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    X = torch.zeros((nsys, n), dtype=torch.float64, device=dev)
+    it = torch.zeros(nsys, dtype=torch.float32, device=dev)
+    cv = torch.zeros(nsys, dtype=torch.int32, device=dev)
+    rs = torch.zeros(nsys, dtype=torch.float64, device=dev)
+    _call(lib().ref_general_isai_solve, n, len(ci), nsys, T(rp, torch.int32), T(ci, torch.int32), T(vals), T(b), X,
+          len(ai[1]), T(ai[0], torch.int32), T(ai[1], torch.int32), T(ai[2]), it, cv, rs)
+    return {"x": X.cpu().numpy(), "iters": it.cpu().numpy(), "conv": cv.cpu().numpy(), "res": rs.cpu().numpy()}
+

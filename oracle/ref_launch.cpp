@@ -16,6 +16,7 @@
 //   ParILU(0)          parILU_0_gpu.cu:274-282                                 (npages x 512, (nL+nU) doubles)
 //   ISAI extraction    isai_gpu.cu:312-317                                     (n x 512)
 //   ISAI fill / solve  isai_gpu.cu:668-675                                     (ceil(32 n npages / 512) x 512)
+//   general ISAI solver PrecondBiCGSTAB_general_isai_gpu.cu:266-274             (npages x 512, static)
 // The spin-waiting ILU approaches 2 and 3 are never launched.
 #include <cuda.h>
 
@@ -26,8 +27,8 @@
 
 namespace {
 
-const char* kUnits[] = {"merged", "ilu_split", "ilu_isai", "ilu0", "parilu", "isai"};
-enum { U_MERGED, U_SPLIT, U_ISAI_SOLVER, U_ILU0, U_PARILU, U_ISAI, U_COUNT };
+const char* kUnits[] = {"merged", "ilu_split", "ilu_isai", "ilu0", "parilu", "isai", "general_isai"};
+enum { U_MERGED, U_SPLIT, U_ISAI_SOLVER, U_ILU0, U_PARILU, U_ISAI, U_GENERAL, U_COUNT };
 CUmodule g_mod[U_COUNT] = {};
 char g_err[512] = "";
 
@@ -167,6 +168,13 @@ int ref_isai_fill(int npages, int n, int* irp, int* ici, double* ivals, int innz
                &matrix_type};
   const unsigned grid = (unsigned)((32LL * n * npages + 511) / 512);
   return launch(U_ISAI, "fill_values_and_solve_kernel_approach1", grid, 512, 0, a);
+}
+
+int ref_general_isai_solve(int n, int nnz, int npages, const int* rp, const int* ci, const double* vals,
+                           const double* rhs, double* ans, int innz, const int* irp, const int* ici, const double* iv,
+                           float* iters, int* conv, double* res) {
+  void* a[] = {&n, &nnz, &npages, &rp, &ci, &vals, &rhs, &ans, &innz, &irp, &ici, &iv, &iters, &conv, &res};
+  return launch(U_GENERAL, "KernelBatchedPreconditionedBiCGSTABGeneralISAI", npages, 512, 0, a);
 }
 
 }  // extern "C"

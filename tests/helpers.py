@@ -33,6 +33,19 @@ def oracle_pipeline(rp, ci, vals, b, precond, approach=1, sweeps=5, fp32=False, 
         return r
     nrp, nci, src = O.add_missing_diag(rp, ci)
     fvals = np.where(src[None, :] >= 0, vals[:, np.maximum(src, 0)], 0.0)
+    if precond == bilu.PRECOND_GENERAL_ISAI:
+        arp, aci = O.isai_pattern(nrp, nci, isai_power)
+        ai = O.isai_values(nrp, nci, fvals, 2, arp, aci)
+        out.update(ai=ai, ai_pattern=(arp, aci))
+        if fp32:
+            r = O.bicgstab(rp, ci, vals, b, prec=O.PREC_GISAI_F32, ail=(arp, aci, None), ail_f32=ai.astype(np.float32),
+                           dot=1, tol_mode=tol_mode, tol=tol, max_iter=max_iter)
+        else:
+            r = O.bicgstab(rp, ci, vals, b, prec=O.PREC_GISAI, ail=(arp, aci, ai), dot=1, tol_mode=tol_mode, tol=tol,
+                           max_iter=max_iter)
+        out.update(r)
+        out["true_res"] = O.true_residual(rp, ci, vals, b, r["x"])
+        return out
     if precond in (bilu.PRECOND_ILU0, bilu.PRECOND_ILU0_SPLIT, bilu.PRECOND_ILU0_ISAI):
         lu = O.ilu0(nrp, nci, fvals, approach)
     else:

@@ -59,6 +59,33 @@ def test_isai_bitwise(cuda, family, precond):
     _compare(g, o, f"ISAI precond {precond} {family}")
 
 
+@pytest.mark.parametrize("family", ["2d5_16x16", "3d7_5x5x5", "cd2d_12x12"])
+@pytest.mark.parametrize("fp32", [False, True])
+def test_general_isai_bitwise(cuda, family, fp32):
+    rp, ci, v, b = H.workload(family, NSYS)
+    kw = dict(tol_mode=1, tol=1e-10) if fp32 else {}
+    o = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_GENERAL_ISAI, fp32=fp32, **kw)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_GENERAL_ISAI,
+                    factor_precision=bilu.FP32 if fp32 else bilu.FP64, **kw)
+    _compare(g, o, f"general ISAI {family} fp32={fp32}")
+    assert np.all(g["conv"] == 1)
+
+
+def test_general_isai_entry_point_bitwise(cuda):
+    import torch
+    rp, ci, v, b = H.workload("cd2d_12x12", NSYS)
+    with bilu.Plan(rp, ci, precond=bilu.PRECOND_GENERAL_ISAI, isai_power=2) as plan:
+        arp, aci = plan.pattern(1)
+        orp, oci = O.isai_pattern(rp, ci, 2)
+        np.testing.assert_array_equal(arp, orp)
+        np.testing.assert_array_equal(aci, oci)
+        V = torch.from_numpy(v).to(cuda)
+        AI = torch.empty((NSYS, len(aci)), dtype=torch.float64, device=cuda)
+        plan.isai(V, AI, None)
+        torch.cuda.synchronize()
+    H.assert_bitwise(AI.cpu().numpy(), O.isai_values(rp, ci, v, 2, orp, oci), "bilu_isai general")
+
+
 @pytest.mark.parametrize("precond", [bilu.PRECOND_ILU0, bilu.PRECOND_PARILU0, bilu.PRECOND_PARILU0_ISAI])
 def test_fp32_factors_bitwise(cuda, precond):
     rp, ci, v, b = H.workload("cd2d_12x12", NSYS)

@@ -96,3 +96,20 @@ def test_reference_parilu_reaches_the_same_fixed_point(cuda, family):
     a3 = O.ilu0(rp, ci, v, 3)
     np.testing.assert_allclose(r, a3, rtol=1e-13, atol=1e-15)
     np.testing.assert_allclose(j, a3, rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("family", ["2d5_8x8", "2d5_16x16", "cd2d_12x12", "3d7_5x5x5"])
+def test_reference_general_isai(cuda, family):
+    """GenerateISAI_gpu(aiA, A, general, 1)'s kernels (Gauss-Jordan with partial pivoting) and the general-ISAI
+    solver kernel, against the oracle and the library."""
+    rp, ci, v, b = H.workload(family, NSYS)
+    arp, aci = O.isai_pattern(rp, ci, 1, v[0])
+    ai = O.isai_values(rp, ci, v, 2, arp, aci)
+    H.assert_bitwise(R.isai(cuda, rp, ci, v, 2, arp, aci), ai, f"reference general ISAI {family}")
+    o = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_GENERAL_ISAI, isai_power=1)
+    _safe(o)
+    r = R.general_isai_solve(cuda, rp, ci, v, b, (arp, aci, ai))
+    _cmp(r, o, f"reference general-ISAI solver {family}")
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_GENERAL_ISAI, isai_power=1)
+    _cmp(g, r, f"library vs reference general-ISAI solver {family}")
+

@@ -33,6 +33,7 @@ def _host(bufs):
     ("2d5_16x16", dict(precond=bilu.PRECOND_ILU0_SPLIT, ilu_approach=1)),
     ("cd2d_12x12", dict(precond=bilu.PRECOND_PARILU0, factor_precision=bilu.FP32, tol_mode=bilu.TOL_REL,
                         tol=1e-10)),
+    ("cd2d_12x12", dict(precond=bilu.PRECOND_GENERAL_ISAI, isai_power=2)),
 ])
 def test_noalloc_matches_bilu_solve_twice(cuda, family, opts):
     import torch
