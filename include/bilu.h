@@ -97,6 +97,12 @@ typedef struct bilu_options {
   double parilu_res_tol;     /* > 0: ParILU sweeps stop once the ILU residual
                                 ||(A - LU)|_S||_F / ||A||_F <= parilu_res_tol (at most
                                 parilu_sweeps sweeps); 0: exactly parilu_sweeps sweeps     */
+  int    isai_lower_diag;    /* bilu_isai only.  0: aiL is the ISAI of the unit lower factor
+                                of ILU factors stored in place (diagonal implicit).  1: the
+                                values at the diagonal positions belong to the lower
+                                triangular matrix itself and aiL divides by them, as
+                                GenerateISAI_gpu(lower_tri) (isai_gpu.cu:325-355) does for a
+                                stand-alone lower triangular matrix.  Solves reject 1.     */
 } bilu_options;
 
 /* Fills *opts with the reference defaults: merged ILU(0), approach 1, 5 sweeps,

@@ -44,6 +44,7 @@ class Options(C.Structure):
         ("tol_mode", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int), ("factor_precision", C.c_int),
         ("reduction", C.c_int), ("compute_true_residual", C.c_int), ("threads_per_system", C.c_int),
         ("parilu_res_tol", C.c_double),
+        ("isai_lower_diag", C.c_int),
     ]
 
 

@@ -1,10 +1,13 @@
-"""Build the in-tree shared library libbilu.so (CUDA kernels + C ABI) for sm_103a.
+"""Build the in-tree shared libraries for sm_103a.
 
 Usage: python merging-ilu0_gb300/bilu_build.py [--force]
 
-Every translation unit under csrc/ is compiled in parallel with nvcc for
-sm_103a only, then linked into merging-ilu0_gb300/libbilu.so.  Objects go to
-merging-ilu0_gb300/_build/ (git-ignored).  Rebuilds only what changed.
+libbilu.so: every translation unit under csrc/ (CUDA kernels + C ABI) is
+compiled in parallel with nvcc for sm_103a only, then linked.
+libbilu_ref.so: the drop-in C++ interface of the original code (shim/: batch
+containers, Matrix Market I/O and the solver entry points), host C++ on top of
+libbilu.so.  Objects go to merging-ilu0_gb300/_build/ (git-ignored).  Rebuilds
+only what changed.
 """
 import concurrent.futures as cf
 import os
@@ -17,6 +20,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbilu.so")
+SHIM = os.path.join(HERE, "shim")
+SHIM_LIB = os.path.join(HERE, "libbilu_ref.so")
 INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -75,9 +80,33 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n$ {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    build_shim(force)
     if verbose:
-        print("built", LIB)
+        print("built", LIB, "and", SHIM_LIB)
     return LIB
+
+
+def _cuda_dirs():
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    libs = [d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib")) if os.path.isdir(d)]
+    return os.path.join(cuda, "include"), libs
+
+
+def build_shim(force=False):
+    """libbilu_ref.so: g++ over shim/*.cpp, linked to libbilu.so (rpath $ORIGIN) and the CUDA runtime."""
+    srcs = sorted(os.path.join(SHIM, f) for f in os.listdir(SHIM) if f.endswith(".cpp"))
+    hdrs = [os.path.join(SHIM, "include", f) for f in os.listdir(os.path.join(SHIM, "include"))]
+    deps = srcs + hdrs + [os.path.join(INCLUDE, "bilu.h"), LIB]
+    if not force and os.path.exists(SHIM_LIB) and os.path.getmtime(SHIM_LIB) >= max(map(os.path.getmtime, deps)):
+        return SHIM_LIB
+    inc, libdirs = _cuda_dirs()
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall",
+           "-I", os.path.join(SHIM, "include"), "-I", INCLUDE, "-I", inc, *srcs, "-o", SHIM_LIB,
+           "-L", HERE, "-lbilu", *[f"-L{d}" for d in libdirs], "-lcudart", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"shim build failed:\n$ {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return SHIM_LIB
 
 
 if __name__ == "__main__":

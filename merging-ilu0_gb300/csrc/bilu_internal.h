@@ -61,6 +61,7 @@ struct DevPattern {
   const int2* ail_prog = nullptr;
   const int* aiu_prog_ptr = nullptr;
   const int2* aiu_prog = nullptr;
+  int l_diag = 0;  // 1: aiL divides by the stored diagonal of a lower triangular matrix
   // general ISAI: per row the sz*sz positions of A(J_k, J_t) in the factor
   // pattern (row-major over k, -1 = structural zero), and the position of i in J
   int gen_maxs = 0;

@@ -81,6 +81,8 @@ extern "C" bilu_status bilu_solve_noalloc(bilu_plan* P, int nsys, const double* 
   if (!P) return set_error(BILU_ERR_INVALID, "bilu_solve_noalloc: NULL plan");
   if (nsys < 0 || (nsys > 0 && (!d_values || !d_b || !d_x)))
     return set_error(BILU_ERR_INVALID, "bilu_solve_noalloc: bad arguments");
+  if (P->opts.isai_lower_diag)
+    return set_error(BILU_ERR_INVALID, "bilu_solve_noalloc: plans with isai_lower_diag = 1 only serve bilu_isai");
   if (nsys == 0) return BILU_OK;
   const bilu_options& o = P->opts;
   const int prec = o.precond;

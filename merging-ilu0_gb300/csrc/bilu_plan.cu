@@ -344,6 +344,7 @@ bilu_status upload(bilu_plan& P) {
   d.mlp_ent = b + o_ment;
   if (P.has_isai) {
     d.ail_nnz = P.ail_rp[P.n];
+    d.l_diag = P.opts.isai_lower_diag ? 1 : 0;
     d.aiu_nnz = P.aiu_rp[P.n];
     d.ail_rp = b + o_alrp;
     d.ail_ci = b + o_alci;
@@ -392,6 +393,7 @@ bilu_status check_opts(const bilu_options* o) {
   if (o->threads_per_system < 0 || o->threads_per_system > 1024)
     return set_error(BILU_ERR_INVALID, "options: threads_per_system must be 0..1024");
   if (!(o->parilu_res_tol >= 0.0)) return set_error(BILU_ERR_INVALID, "options: parilu_res_tol must be >= 0");
+  if (o->isai_lower_diag != 0 && o->isai_lower_diag != 1) return set_error(BILU_ERR_INVALID, "options: isai_lower_diag");
   return BILU_OK;
 }
 
@@ -418,6 +420,7 @@ void bilu_default_options(bilu_options* o) {
   o->compute_true_residual = 1;
   o->threads_per_system = 0;
   o->parilu_res_tol = 0.0;
+  o->isai_lower_diag = 0;
 }
 
 const char* bilu_last_error(void) { return g_last_error.c_str(); }
@@ -653,6 +656,8 @@ int fact_threads(const bilu_plan* P) { return std::min(512, round_up(std::max(P-
 bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double* lu_init, const double* b, double* x,
                        const bilu_results* R, cudaStream_t st) {
   if (nsys < 0 || (nsys > 0 && (!vals || !b || !x))) return set_error(BILU_ERR_INVALID, "bilu_solve: bad arguments");
+  if (P->opts.isai_lower_diag)
+    return set_error(BILU_ERR_INVALID, "bilu_solve: plans with isai_lower_diag = 1 only serve bilu_isai");
   if (nsys == 0) return BILU_OK;
   const bilu_options& o = P->opts;
   const bool fp32 = is_fp32(o);

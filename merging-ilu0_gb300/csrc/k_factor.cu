@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const int beg = __ldg(P.ail_rp + i), sz = __ldg(P.ail_rp + i + 1) - beg;
     double* m = M + beg;
-    m[sz - 1] = 1.0;
+    m[sz - 1] = P.l_diag ? 1.0 / LU[__ldg(P.diag + i)] : 1.0;
     int q = __ldg(P.ail_prog_ptr + i);
     for (int blk = 0; blk < sz - 1; ++blk) {
       const int2 h = __ldg(P.ail_prog + q++);  // {t, count}
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
         const int2 e = __ldg(P.ail_prog + q++);  // {c, position in LU}
         acc = fma(-m[e.x], LU[e.y], acc);
       }
-      m[h.x] = acc;
+      m[h.x] = P.l_diag ? acc / LU[__ldg(P.diag + __ldg(P.ail_ci + beg + h.x))] : acc;
     }
   }
   __syncthreads();
