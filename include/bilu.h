@@ -151,6 +151,10 @@ typedef struct bilu_plan_info {
   int threads;           /* CTA size used per system by the solver kernel          */
   int smem_bytes;        /* dynamic shared memory per system of the solver kernel  */
   int operands_in_smem;  /* bit 0: A, bit 1: factors / aiL, bit 2: aiU in shared memory */
+  int solver_kernel;     /* 0: one CTA per system, vectors in shared memory (every mode);
+                            1: register-resident (BILU_REDUCE_FAST with ISAI or no
+                            preconditioner, n <= 2048): `threads` threads per system,
+                            each owning rows t + k * threads                         */
 } bilu_plan_info;
 bilu_status bilu_plan_get_info(const bilu_plan* plan, bilu_plan_info* info);
 

@@ -57,7 +57,7 @@ class Results(C.Structure):
 class PlanInfo(C.Structure):
     _fields_ = [(k, C.c_int) for k in (
         "n", "nnz", "nnz_in", "missing_diag", "nnz_L", "nnz_U", "nnz_isai_L", "nnz_isai_U", "levels_lower",
-        "levels_upper", "max_row_len", "threads", "smem_bytes", "operands_in_smem")]
+        "levels_upper", "max_row_len", "threads", "smem_bytes", "operands_in_smem", "solver_kernel")]
 
 
 class Timing(C.Structure):

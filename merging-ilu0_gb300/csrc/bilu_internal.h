@@ -164,6 +164,14 @@ __host__ __device__ inline SmemLayout layout_for(int n, int annz, int fnnz, int 
   return L;
 }
 
+// Shared-memory carve-up of the register-resident FAST solver (k_solve_rr.cu):
+// reduction slots, the SpMV input (FP64), the preconditioner input and
+// intermediate (FT), then optionally A and the ISAI values.  -1 = not used /
+// read from global memory.
+struct RRLayout {
+  int red = -1, ph = -1, in = -1, mid = -1, A = -1, ail = -1, aiu = -1, total = 0;
+};
+
 // One system of an uneven batch (own size and pattern); offsets in ints into
 // the plan's metadata buffer, value / vector offsets into the concatenated
 // batch arrays.
@@ -189,6 +197,11 @@ void* uneven_kernel(int fp32, int reduce_fast, int maxl);
 cudaError_t launch_uneven(const UnevenArgs& u, int threads, int grid, int fp32, int reduce_fast, int maxl,
                           cudaStream_t st);
 cudaError_t launch_solve(const SolveArgs& a, int threads, int fp32, int reduce_fast, int maxl, cudaStream_t st);
+// register-resident FAST solver: pv 0 none, 1 ISAI of L and U, 2 general ISAI
+int rr_rows_per_thread(int n, int nt);  // smallest R in {1, 2, 4, 8} with R * nt >= n, else 0
+int rr_max_threads(int R);
+const void* rr_kernel(int pv, int fp32, int R);
+cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, cudaStream_t st);
 size_t solve_max_smem();
 cudaError_t launch_expand(const DevPattern& p, int nsys, const double* vin, double* vout, cudaStream_t st);
 cudaError_t launch_ilu0(const DevPattern& p, int nsys, const double* A, double* lu, int approach, int threads,
@@ -247,6 +260,10 @@ struct bilu_plan {
   // solver kernel configuration
   int threads = 0;
   bilu::SmemLayout lay;
+  // register-resident FAST solver (k_solve_rr.cu), when it applies
+  bool rr = false;
+  int rr_threads = 0, rr_pv = 0;
+  bilu::RRLayout rr_lay;
   // workspace
   void* ws = nullptr;
   size_t ws_bytes = 0;

@@ -273,6 +273,61 @@ void choose_layout(bilu_plan& P) {
   P.threads = th;
 }
 
+// Register-resident FAST solver: FAST order, ISAI or no preconditioner, at most
+// 8 rows per thread.  Threads per system: the caller's, else the fewest warps
+// that give every thread at most 8 rows (one warp for n <= 256).  Shared memory
+// beyond the mandatory part (reductions, SpMV input, preconditioner scratch)
+// holds A, then aiL, then aiU, while the CTA still fits as many times per SM
+// as its registers and threads allow.
+void choose_rr(bilu_plan& P) {
+  const bilu_options& o = P.opts;
+  P.rr = false;
+  const int pk = prec_kind(o.precond);
+  if (o.reduction != BILU_REDUCE_FAST || (pk != PK_ISAI && pk != PK_NONE)) return;
+  const int n = P.n;
+  int nt = o.threads_per_system > 0 ? round_up(o.threads_per_system, 32) : round_up((n + 7) / 8, 32);
+  nt = std::max(nt, 32);
+  const int R = rr_rows_per_thread(n, nt);
+  if (R == 0 || nt > rr_max_threads(R)) return;
+  const int pv = pk == PK_NONE ? 0 : (P.general_isai ? 2 : 1);
+  const bool fp32 = is_fp32(o);
+  const int fts = fp32 ? 4 : 8;
+  RRLayout L;
+  int off = 0;
+  auto take = [&](int& dst, long long bytes) {
+    dst = off;
+    off = (int)((off + bytes + 15) & ~15LL);
+  };
+  take(L.red, 4 * 64 * 8);
+  take(L.ph, (long long)n * 8);
+  if (pv != 0) take(L.in, (long long)n * fts);
+  if (pv == 1) take(L.mid, (long long)n * fts);
+  int dev = 0, per_sm = 0, reserved = 0, optin = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const void* k = rr_kernel(pv, fp32 ? 1 : 0, R);
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(optin, off)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, nt, off) != cudaSuccess || occ < 1) {
+    cudaGetLastError();
+    return;
+  }
+  const int budget = std::min(optin, per_sm / occ - reserved);
+  if (off > budget) return;
+  auto stage = [&](int& dst, long long bytes) {
+    if (bytes > 0 && off + bytes <= budget) take(dst, bytes);
+  };
+  stage(L.A, (long long)P.nnz_in * 8);
+  if (pv != 0) stage(L.ail, (long long)P.ail_rp[n] * fts);
+  if (pv == 1) stage(L.aiu, (long long)P.aiu_rp[n] * fts);
+  L.total = off;
+  P.rr = true;
+  P.rr_threads = nt;
+  P.rr_pv = pv;
+  P.rr_lay = L;
+}
+
 bilu_status upload(bilu_plan& P) {
   std::vector<int> buf;
   auto put = [&](const std::vector<int>& v) {
@@ -542,7 +597,8 @@ bilu_status bilu_plan_create(bilu_plan** out, int n, int nnz, const int* h_rp, c
     }
   }
   choose_layout(*P);
-  if (P->lay.total > (int)solve_max_smem()) {
+  choose_rr(*P);
+  if (!P->rr && P->lay.total > (int)solve_max_smem()) {
     const int need = P->lay.total;
     delete P;
     return set_error(BILU_ERR_CAPACITY, "solver needs " + std::to_string(need) + " bytes of shared memory per system");
@@ -607,6 +663,12 @@ bilu_status bilu_plan_get_info(const bilu_plan* P, bilu_plan_info* info) {
   info->smem_bytes = P->lay.total;
   info->operands_in_smem = (P->lay.A >= 0 ? 1 : 0) | ((P->lay.F >= 0 || P->lay.ail >= 0) ? 2 : 0) |
                            (P->lay.aiu >= 0 ? 4 : 0);
+  info->solver_kernel = P->rr ? 1 : 0;
+  if (P->rr) {
+    info->threads = P->rr_threads;
+    info->smem_bytes = P->rr_lay.total;
+    info->operands_in_smem = (P->rr_lay.A >= 0 ? 1 : 0) | (P->rr_lay.ail >= 0 ? 2 : 0) | (P->rr_lay.aiu >= 0 ? 4 : 0);
+  }
   return BILU_OK;
 }
 
@@ -753,7 +815,8 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
     }
   }
   if (P->timing) cudaEventRecord(P->ev[1], st);
-  e = launch_solve(a, P->threads, fp32 ? 1 : 0, o.reduction == BILU_REDUCE_FAST ? 1 : 0, maxl, st);
+  e = P->rr ? launch_solve_rr(a, P->rr_lay, P->rr_threads, P->rr_pv, fp32 ? 1 : 0, st)
+            : launch_solve(a, P->threads, fp32 ? 1 : 0, o.reduction == BILU_REDUCE_FAST ? 1 : 0, maxl, st);
   if (e != cudaSuccess) return cuda_err(e, "solver launch");
   if (P->timing) cudaEventRecord(P->ev[2], st);
   return BILU_OK;

@@ -1,0 +1,378 @@
+// Register-resident batched BiCGSTAB for BILU_REDUCE_FAST with an ISAI
+// preconditioner (two triangles or the general ISAI of A) or none.
+//
+// Same method, exits and iteration counting as the shared-memory kernel
+// (k_solve.cu, after PrecondBiCGSTAB_ilu_isai_gpu.cu:89-257 and
+// Bicgstab_common.hpp:195-250); only the reduction order differs, and it is
+// fixed by (threads per system, rows per thread), so the oracle restates it
+// bit for bit (orc_bicgstab_fast).
+//
+// GB300 mapping.  FP64 issue is the bound (about two FP64 lane-operations per
+// clock per SM, one warp instruction costs the same whatever its active
+// mask), and the shared-memory kernel loses most of it to serialisation: one
+// 200 KB CTA per SM, warp-0 inner products (32 dependent FMAs at n = 1000) and
+// ~15 block barriers per iteration during which the SM's FP64 pipes idle.
+// Here:
+//   * thread t of an NT-thread CTA owns rows t + k*NT, k < R (R <= 8); the
+//     vectors x, r/s, p, v and t live in its registers (r_hat = b is re-read
+//     through L1, p_hat / s_hat are read back from shared memory);
+//   * shared memory holds only what other rows read: the SpMV input p_hat /
+//     s_hat (FP64), the preconditioner input and intermediate (FT), and, when
+//     they fit without costing occupancy, A and the ISAI values;
+//   * the six inner products of an iteration run as four block reductions
+//     (xor-butterfly within each warp, then every thread sums the per-warp
+//     partials in warp order), so all threads hold identical scalars and take
+//     identical branches without a broadcast barrier; 9 barriers per iteration;
+//   * the CTA is small (one warp for n <= 256), so several systems share an SM
+//     and one system's barrier or reduction latency overlaps another's FMAs;
+//   * with FP32 ISAI values (BILU_FP32) both preconditioner SpMVs run on the
+//     FP32 pipe; FP64 stays in A*x, the inner products and the recurrences.
+//
+// Reduction order (what orc_bicgstab_fast restates):
+//   thread partial   d = fma(a_i, b_i, d) over its rows in k order, from 0.0
+//   warp             lane values v_l; for off = 16, 8, 4, 2, 1: v_l = v_l + v_(l^off); lane 0's value
+//   block            s = 0.0; s = s + w_j for warps j = 0 .. NT/32-1
+//   SpMV row         acc = fma(a_k, x_ci(k), acc), k ascending, from 0.0 (FP64)
+//   ISAI row (FT)    the same in FT; input rounded to FT, output widened to FP64
+#include <cuda_runtime.h>
+
+#include "bilu_internal.h"
+
+namespace bilu {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// K values summed over the CTA; every thread returns the same sums.
+// red: K * 32 doubles of this reduction's own slot.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double* red, int nw) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v[k] = v[k] + __shfl_xor_sync(kFull, v[k], off);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) red[k * 32 + warp] = v[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s = s + red[k * 32 + w];
+    v[k] = s;
+  }
+}
+
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+
+template <typename VT, typename XT>
+__device__ __forceinline__ XT row_acc(const VT* __restrict__ val, const int* __restrict__ ci, int beg, int end,
+                                      const XT* __restrict__ xv) {
+  XT acc = XT(0);
+  for (int k = beg; k < end; ++k) acc = fma_t((XT)val[k], xv[__ldg(ci + k)], acc);
+  return acc;
+}
+
+// PV: 0 none, 1 ISAI of L and U (z = aiU (aiL v)), 2 general ISAI (z = aiA v).
+// FT: type of the ISAI values and of the preconditioner arithmetic.
+template <int R, int PV, typename FT>
+__global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : 256), 1)
+    k_bicgstab_rr(const SolveArgs a, const RRLayout L) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sys = blockIdx.x;
+  if (sys >= a.nsys) return;
+  const DevPattern& P = a.pat;
+  const int n = P.n, nt = blockDim.x, tid = threadIdx.x, nw = nt >> 5;
+  const int* __restrict__ arp = P.a_rp;
+  const int* __restrict__ aci = P.a_ci;
+  const double* Ag = a.A + (size_t)sys * P.a_nnz;
+  const double* bg = a.b + (size_t)sys * n;
+
+  double* red = reinterpret_cast<double*>(smem + L.red);  // 4 slots of 2 * 32
+  double* sph = reinterpret_cast<double*>(smem + L.ph);
+  FT* sin = reinterpret_cast<FT*>(smem + L.in);
+  FT* smid = reinterpret_cast<FT*>(smem + L.mid);
+
+  const double* Am = Ag;
+  if (L.A >= 0) {
+    double* s = reinterpret_cast<double*>(smem + L.A);
+    for (int k = tid; k < P.a_nnz; k += nt) s[k] = __ldg(Ag + k);
+    Am = s;
+  }
+  const FT* AIL = nullptr;
+  const FT* AIU = nullptr;
+  if (PV != 0) {
+    const FT* g = reinterpret_cast<const FT*>(a.ail) + (size_t)sys * P.ail_nnz;
+    if (L.ail >= 0) {
+      FT* s = reinterpret_cast<FT*>(smem + L.ail);
+      for (int k = tid; k < P.ail_nnz; k += nt) s[k] = g[k];
+      AIL = s;
+    } else {
+      AIL = g;
+    }
+  }
+  if (PV == 1) {
+    const FT* g = reinterpret_cast<const FT*>(a.aiu) + (size_t)sys * P.aiu_nnz;
+    if (L.aiu >= 0) {
+      FT* s = reinterpret_cast<FT*>(smem + L.aiu);
+      for (int k = tid; k < P.aiu_nnz; k += nt) s[k] = g[k];
+      AIU = s;
+    } else {
+      AIU = g;
+    }
+  }
+
+  // registers: x, r (s in the middle of an iteration), p, v, t; r_hat = b is
+  // re-read from global memory (L1) and p_hat / s_hat from shared memory
+  double x[R], r[R], p[R], v[R], t[R];
+  double q[1] = {0.0};
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int i = tid + k * nt;
+    const double bi = i < n ? __ldg(bg + i) : 0.0;
+    x[k] = 0.0;
+    p[k] = 0.0;
+    v[k] = 0.0;
+    t[k] = 0.0;
+    r[k] = bi;
+    if (i < n) q[0] = fma(bi, bi, q[0]);
+  }
+  // ||b||^2 = (r, r_hat) at the start: one reduction serves both (its barrier
+  // also completes the staging above)
+  block_sum<1>(q, red, nw);
+  const double bnorm = sqrt(q[0]);
+  const double thr = (a.tol_mode == BILU_TOL_ABS) ? a.tol : a.tol * bnorm;
+  double rho = q[0], rho_old = 1.0, alpha = 1.0, omega_old = 1.0, res = bnorm;
+  float iter = 0.0f;
+  int status = BILU_SYS_MAX_ITER;
+  bool stop = false;
+  if (bnorm == 0.0) {
+    res = 0.0;
+    status = BILU_SYS_ZERO_RHS;
+    stop = true;
+  } else if (bnorm < thr) {
+    status = BILU_SYS_INITIAL_OK;
+    stop = true;
+  }
+
+// z = M in for this thread's rows.  The input is in `sin` (sph for PV 0),
+// made visible by a barrier; z lands in sph, followed by a barrier.
+#define BILU_RR_APPLY()                                                                                          \
+  do {                                                                                                           \
+    if (PV == 1) {                                                                                               \
+      _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
+        const int i = tid + k * nt;                                                                              \
+        if (i < n) smid[i] = row_acc(AIL, P.ail_ci, __ldg(P.ail_rp + i), __ldg(P.ail_rp + i + 1), sin);          \
+      }                                                                                                          \
+      __syncthreads();                                                                                           \
+      _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
+        const int i = tid + k * nt;                                                                              \
+        if (i < n) sph[i] = (double)row_acc(AIU, P.aiu_ci, __ldg(P.aiu_rp + i), __ldg(P.aiu_rp + i + 1), smid); \
+      }                                                                                                          \
+      __syncthreads();                                                                                           \
+    } else if (PV == 2) {                                                                                        \
+      _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
+        const int i = tid + k * nt;                                                                              \
+        if (i < n) sph[i] = (double)row_acc(AIL, P.ail_ci, __ldg(P.ail_rp + i), __ldg(P.ail_rp + i + 1), sin);   \
+      }                                                                                                          \
+      __syncthreads();                                                                                           \
+    }                                                                                                            \
+  } while (0)
+// writes this thread's rows of `vec` as the preconditioner input
+#define BILU_RR_INPUT(vec)                       \
+  do {                                           \
+    _Pragma("unroll") for (int k = 0; k < R; ++k) { \
+      const int i = tid + k * nt;                \
+      if (i < n) {                               \
+        if (PV == 0)                             \
+          sph[i] = vec[k];                       \
+        else                                     \
+          sin[i] = (FT)vec[k];                   \
+      }                                          \
+    }                                            \
+  } while (0)
+
+  const float max_iter = (float)a.max_iter;
+  while (!stop && iter < max_iter) {
+    if (rho == 0.0) {
+      status = BILU_SYS_BREAKDOWN_RHO;
+      break;
+    }
+    const double beta = (rho / rho_old) * (alpha / omega_old);
+#pragma unroll
+    for (int k = 0; k < R; ++k) p[k] = fma(beta, fma(-omega_old, v[k], p[k]), r[k]);
+    BILU_RR_INPUT(p);
+    __syncthreads();
+    BILU_RR_APPLY();  // p_hat in sph
+    // v = A p_hat, (r_hat, v)
+    q[0] = 0.0;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const int i = tid + k * nt;
+      if (i < n) {
+        v[k] = row_acc(Am, aci, __ldg(arp + i), __ldg(arp + i + 1), sph);
+        q[0] = fma(__ldg(bg + i), v[k], q[0]);
+      }
+    }
+    block_sum<1>(q, red + 64, nw);
+    alpha = rho / q[0];
+    // x += alpha p_hat, s = r - alpha v, ||s||.  p_hat is read before anyone
+    // rewrites sph (PV 0 rewrites it with s right here, after the reduction's
+    // barrier has ended every SpMV read).
+    q[0] = 0.0;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const int i = tid + k * nt;
+      if (i < n) {
+        x[k] = fma(alpha, sph[i], x[k]);
+        r[k] = fma(-alpha, v[k], r[k]);
+        q[0] = fma(r[k], r[k], q[0]);
+      }
+    }
+    BILU_RR_INPUT(r);
+    block_sum<1>(q, red + 128, nw);
+    res = sqrt(q[0]);
+    iter = iter + 0.5f;
+    if (res < thr) {
+      status = BILU_SYS_CONVERGED;
+      break;
+    }
+    BILU_RR_APPLY();  // s_hat in sph
+    // t = A s_hat, (t, s), (t, t)
+    double q2[2] = {0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const int i = tid + k * nt;
+      if (i < n) {
+        t[k] = row_acc(Am, aci, __ldg(arp + i), __ldg(arp + i + 1), sph);
+        q2[0] = fma(t[k], r[k], q2[0]);
+        q2[1] = fma(t[k], t[k], q2[1]);
+      }
+    }
+    block_sum<2>(q2, red + 192, nw);
+    const double omega = q2[0] / q2[1];
+    // x += omega s_hat, r = s - omega t, ||r||, next rho = (r, r_hat)
+    q2[0] = 0.0;
+    q2[1] = 0.0;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const int i = tid + k * nt;
+      if (i < n) {
+        x[k] = fma(omega, sph[i], x[k]);
+        r[k] = fma(-omega, t[k], r[k]);
+        q2[0] = fma(r[k], r[k], q2[0]);
+        q2[1] = fma(__ldg(bg + i), r[k], q2[1]);
+      }
+    }
+    block_sum<2>(q2, red, nw);
+    res = sqrt(q2[0]);
+    iter = iter + 0.5f;
+    rho_old = rho;
+    omega_old = omega;
+    rho = q2[1];
+    if (res < thr) {
+      status = BILU_SYS_CONVERGED;
+      break;
+    }
+  }
+#undef BILU_RR_APPLY
+#undef BILU_RR_INPUT
+
+  // ---- write back
+  double* xg = a.x + (size_t)sys * n;
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int i = tid + k * nt;
+    if (i < n) xg[i] = x[k];
+  }
+  if (tid == 0) {
+    int st = status;
+    if (st == BILU_SYS_MAX_ITER && !isfinite(res)) st = BILU_SYS_NONFINITE;
+    const bool ok = (st == BILU_SYS_CONVERGED || st == BILU_SYS_ZERO_RHS || st == BILU_SYS_INITIAL_OK);
+    if (a.iters) a.iters[sys] = iter;
+    if (a.conv) a.conv[sys] = ok ? 1 : -1;
+    if (a.res) a.res[sys] = res;
+    if (a.status) a.status[sys] = st;
+  }
+  // ---- true residual ||b - A x||: x through shared memory, same reduction order
+  if (a.true_res) {
+    __syncthreads();  // every reader of sph is done
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const int i = tid + k * nt;
+      if (i < n) sph[i] = x[k];
+    }
+    __syncthreads();
+    q[0] = 0.0;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const int i = tid + k * nt;
+      if (i < n) {
+        const double ri = __ldg(bg + i) - row_acc(Am, aci, __ldg(arp + i), __ldg(arp + i + 1), sph);
+        q[0] = fma(ri, ri, q[0]);
+      }
+    }
+    block_sum<1>(q, red + 64, nw);
+    if (tid == 0) a.true_res[sys] = sqrt(q[0]);
+  }
+}
+
+template <int R, int PV, typename FT>
+cudaError_t launch_rr_t(const SolveArgs& a, const RRLayout& L, int nt, cudaStream_t st) {
+  auto k = k_bicgstab_rr<R, PV, FT>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total);
+  if (e != cudaSuccess) return e;
+  k<<<a.nsys, nt, L.total, st>>>(a, L);
+  return cudaGetLastError();
+}
+
+template <int PV, typename FT>
+const void* rr_kernel_pv(int R) {
+  switch (R) {
+    case 1: return (const void*)k_bicgstab_rr<1, PV, FT>;
+    case 2: return (const void*)k_bicgstab_rr<2, PV, FT>;
+    case 4: return (const void*)k_bicgstab_rr<4, PV, FT>;
+    default: return (const void*)k_bicgstab_rr<8, PV, FT>;
+  }
+}
+
+template <int PV, typename FT>
+cudaError_t launch_rr_pv(const SolveArgs& a, const RRLayout& L, int nt, int R, cudaStream_t st) {
+  switch (R) {
+    case 1: return launch_rr_t<1, PV, FT>(a, L, nt, st);
+    case 2: return launch_rr_t<2, PV, FT>(a, L, nt, st);
+    case 4: return launch_rr_t<4, PV, FT>(a, L, nt, st);
+    default: return launch_rr_t<8, PV, FT>(a, L, nt, st);
+  }
+}
+
+}  // namespace
+
+int rr_rows_per_thread(int n, int nt) {
+  for (int R : {1, 2, 4, 8})
+    if ((long long)R * nt >= n) return R;
+  return 0;
+}
+
+int rr_max_threads(int R) { return R <= 1 ? 1024 : (R == 2 ? 512 : 256); }
+
+const void* rr_kernel(int pv, int fp32, int R) {
+  if (pv == 0) return rr_kernel_pv<0, double>(R);
+  if (pv == 1) return fp32 ? rr_kernel_pv<1, float>(R) : rr_kernel_pv<1, double>(R);
+  return fp32 ? rr_kernel_pv<2, float>(R) : rr_kernel_pv<2, double>(R);
+}
+
+cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, cudaStream_t st) {
+  if (a.nsys == 0) return cudaSuccess;
+  const int R = rr_rows_per_thread(a.pat.n, nt);
+  if (R == 0 || nt % 32 || nt > rr_max_threads(R)) return cudaErrorInvalidConfiguration;
+  if (pv == 0) return launch_rr_pv<0, double>(a, L, nt, R, st);
+  if (pv == 1) return fp32 ? launch_rr_pv<1, float>(a, L, nt, R, st) : launch_rr_pv<1, double>(a, L, nt, R, st);
+  return fp32 ? launch_rr_pv<2, float>(a, L, nt, R, st) : launch_rr_pv<2, double>(a, L, nt, R, st);
+}
+
+}  // namespace bilu

@@ -286,8 +286,11 @@ ORC_API void orc_ilu0(int n, int nnz, const int* rp, const int* ci, int nsys, co
 // (every entry of sweep t+1 reads the values of sweep t).  Initial guess
 // (Fill_L_and_U, factorization.cu:288-344): L = strict-lower(A) + I,
 // U = upper(A), i.e. the in-place factors start equal to A; `init` overrides.
-ORC_API void orc_parilu0(int n, int nnz, const int* rp, const int* ci, int nsys, const double* vals,
-                         const double* init, int sweeps, double* lu) {
+// fast = 1: the library's BILU_REDUCE_FAST sweep (k_parilu0<true>): lower
+// entries are multiplied by the reciprocals 1 / u_jj of the current diagonal,
+// formed once per sweep, instead of divided.
+ORC_API void orc_parilu0_ex(int n, int nnz, const int* rp, const int* ci, int nsys, const double* vals,
+                            const double* init, int sweeps, double* lu, int fast) {
   std::vector<int> diag(n);
   orc_find_diag(n, rp, ci, diag.data());
   // dependency lists (pattern only)
@@ -314,19 +317,26 @@ ORC_API void orc_parilu0(int n, int nnz, const int* rp, const int* ci, int nsys,
     const double* A = vals + (size_t)s * nnz;
     double* cur = lu + (size_t)s * nnz;
     std::memcpy(cur, init ? init + (size_t)s * nnz : A, sizeof(double) * nnz);
-    std::vector<double> nxt(nnz);
+    std::vector<double> nxt(nnz), rinv(n);
     for (int t = 0; t < sweeps; ++t) {
+      if (fast)
+        for (int r = 0; r < n; ++r) rinv[r] = 1.0 / cur[diag[r]];
       for (int e = 0; e < nnz; ++e) {
         double sum = 0.0;
         for (int q = dptr[e]; q < dptr[e + 1]; ++q) sum = std::fma(cur[dl[q]], cur[du[q]], sum);
         double v = A[e] - sum;
         const int i = rowof[e], j = ci[e];
-        if (j < i) v = v / cur[diag[j]];
+        if (j < i) v = fast ? v * rinv[j] : v / cur[diag[j]];
         nxt[e] = v;
       }
       std::memcpy(cur, nxt.data(), sizeof(double) * nnz);
     }
   }
+}
+
+ORC_API void orc_parilu0(int n, int nnz, const int* rp, const int* ci, int nsys, const double* vals,
+                         const double* init, int sweeps, double* lu) {
+  orc_parilu0_ex(n, nnz, rp, ci, nsys, vals, init, sweeps, lu, 0);
 }
 
 // ||(A - L U)|_S||_F / ||A||_F on the factor pattern S (the ILU residual that
@@ -637,6 +647,173 @@ ORC_API void orc_bicgstab(int n, int nnz, const int* rp, const int* ci, int nsys
 
 // KernelFillTrueResNorms (Bicgstab_common.hpp:294-342): r = b - A x with the
 // SpMV tree order, norm = sqrt of the SERIAL inner product.
+// BILU_REDUCE_FAST BiCGSTAB of the register-resident kernel (k_solve_rr.cu)
+// with `nt` threads per system, thread t owning rows t + k*nt: the same
+// recurrences, exits and iteration counting as orc_bicgstab, in this order --
+//   thread partial   fma over the thread's rows in k order, from 0.0
+//   warp             xor butterfly v_l = v_l + v_(l^off), off = 16..1; lane 0
+//   block            0.0 + w_0 + w_1 + ... over the warps in order
+//   rows             A*x and the ISAI rows: fma over the row, from 0.0; ISAI in
+//                    float when fp32 (input rounded, output widened)
+// pv: 0 none, 1 z = aiU (aiL v), 2 z = aiA v.  No reference counterpart.
+namespace {
+
+double fast_block_sum(const std::vector<double>& part, int nt) {
+  double s = 0.0;
+  for (int w = 0; w < nt / 32; ++w) {
+    double v[32], nv[32];
+    for (int l = 0; l < 32; ++l) v[l] = part[32 * w + l];
+    for (int off = 16; off >= 1; off >>= 1) {
+      for (int l = 0; l < 32; ++l) nv[l] = v[l] + v[l ^ off];
+      for (int l = 0; l < 32; ++l) v[l] = nv[l];
+    }
+    s = s + v[0];
+  }
+  return s;
+}
+
+template <typename T>
+T fast_row(const int* rp, const int* ci, const T* val, int i, const T* x) {
+  T acc = T(0);
+  for (int k = rp[i]; k < rp[i + 1]; ++k) acc = std::fma(val[k], x[ci[k]], acc);
+  return acc;
+}
+
+}  // namespace
+
+ORC_API int orc_bicgstab_fast(int n, int nnz, const int* rp, const int* ci, int nsys, const double* A,
+                              const double* b, int pv, int fp32, const int* l_rp, const int* l_ci, int l_nnz,
+                              const double* l_vals, const float* l_vals32, const int* u_rp, const int* u_ci, int u_nnz,
+                              const double* u_vals, const float* u_vals32, int nt, int tol_mode, double tol,
+                              int max_iter, double* x_out, float* iters, int* conv, double* res_out, int* status_out,
+                              double* true_res) {
+  if (nt <= 0 || nt % 32) return -1;
+  int R = 0;
+  for (int c : {1, 2, 4, 8})
+    if (!R && (long long)c * nt >= n) R = c;
+  if (!R) return -1;
+  // bilu.h BILU_SYS_* values
+  constexpr int kConverged = 1, kMaxIter = -1, kBreakdown = -2, kNonfinite = -3, kZeroRhs = 2, kInitialOk = 3;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int s = 0; s < nsys; ++s) {
+    const double* As = A + (size_t)s * nnz;
+    const double* bs = b + (size_t)s * n;
+    const double* Ld = l_vals ? l_vals + (size_t)s * l_nnz : nullptr;
+    const float* Lf = l_vals32 ? l_vals32 + (size_t)s * l_nnz : nullptr;
+    const double* Ud = u_vals ? u_vals + (size_t)s * u_nnz : nullptr;
+    const float* Uf = u_vals32 ? u_vals32 + (size_t)s * u_nnz : nullptr;
+    std::vector<double> x(n, 0.0), r(bs, bs + n), p(n, 0.0), v(n, 0.0), t(n, 0.0), sph(n, 0.0), part(nt);
+    std::vector<double> ind(n), midd(n);
+    std::vector<float> inf(n), midf(n);
+    // per-thread partial sums of f(i) over thread t's rows
+    auto reduce = [&](auto f) {
+      for (int th = 0; th < nt; ++th) {
+        double d = 0.0;
+        for (int k = 0; k < R; ++k) {
+          const int i = th + k * nt;
+          if (i < n) d = f(i, d);
+        }
+        part[th] = d;
+      }
+      return fast_block_sum(part, nt);
+    };
+    // z = M in into sph
+    auto apply = [&](const std::vector<double>& in) {
+      if (pv == 0) {
+        sph = in;
+      } else if (fp32) {
+        for (int i = 0; i < n; ++i) inf[i] = (float)in[i];
+        if (pv == 1) {
+          for (int i = 0; i < n; ++i) midf[i] = fast_row<float>(l_rp, l_ci, Lf, i, inf.data());
+          for (int i = 0; i < n; ++i) sph[i] = (double)fast_row<float>(u_rp, u_ci, Uf, i, midf.data());
+        } else {
+          for (int i = 0; i < n; ++i) sph[i] = (double)fast_row<float>(l_rp, l_ci, Lf, i, inf.data());
+        }
+      } else {
+        if (pv == 1) {
+          for (int i = 0; i < n; ++i) midd[i] = fast_row<double>(l_rp, l_ci, Ld, i, in.data());
+          for (int i = 0; i < n; ++i) sph[i] = fast_row<double>(u_rp, u_ci, Ud, i, midd.data());
+        } else {
+          for (int i = 0; i < n; ++i) sph[i] = fast_row<double>(l_rp, l_ci, Ld, i, in.data());
+        }
+      }
+    };
+    const double q0 = reduce([&](int i, double d) { return std::fma(bs[i], bs[i], d); });
+    const double bnorm = std::sqrt(q0);
+    const double thr = tol_mode == 0 ? tol : tol * bnorm;
+    double rho = q0, rho_old = 1.0, alpha = 1.0, omega_old = 1.0, res = bnorm;
+    float iter = 0.0f;
+    int status = kMaxIter;
+    bool stop = false;
+    if (bnorm == 0.0) {
+      res = 0.0;
+      status = kZeroRhs;
+      stop = true;
+    } else if (bnorm < thr) {
+      status = kInitialOk;
+      stop = true;
+    }
+    const float fmax = (float)max_iter;
+    while (!stop && iter < fmax) {
+      if (rho == 0.0) {
+        status = kBreakdown;
+        break;
+      }
+      const double beta = (rho / rho_old) * (alpha / omega_old);
+      for (int i = 0; i < n; ++i) p[i] = std::fma(beta, std::fma(-omega_old, v[i], p[i]), r[i]);
+      apply(p);
+      for (int i = 0; i < n; ++i) v[i] = fast_row<double>(rp, ci, As, i, sph.data());
+      const double rv = reduce([&](int i, double d) { return std::fma(bs[i], v[i], d); });
+      alpha = rho / rv;
+      for (int i = 0; i < n; ++i) {
+        x[i] = std::fma(alpha, sph[i], x[i]);
+        r[i] = std::fma(-alpha, v[i], r[i]);
+      }
+      const double ss = reduce([&](int i, double d) { return std::fma(r[i], r[i], d); });
+      res = std::sqrt(ss);
+      iter = iter + 0.5f;
+      if (res < thr) {
+        status = kConverged;
+        break;
+      }
+      apply(r);
+      for (int i = 0; i < n; ++i) t[i] = fast_row<double>(rp, ci, As, i, sph.data());
+      const double ts = reduce([&](int i, double d) { return std::fma(t[i], r[i], d); });
+      const double tt = reduce([&](int i, double d) { return std::fma(t[i], t[i], d); });
+      const double omega = ts / tt;
+      for (int i = 0; i < n; ++i) {
+        x[i] = std::fma(omega, sph[i], x[i]);
+        r[i] = std::fma(-omega, t[i], r[i]);
+      }
+      const double rr = reduce([&](int i, double d) { return std::fma(r[i], r[i], d); });
+      const double rhr = reduce([&](int i, double d) { return std::fma(bs[i], r[i], d); });
+      res = std::sqrt(rr);
+      iter = iter + 0.5f;
+      rho_old = rho;
+      omega_old = omega;
+      rho = rhr;
+      if (res < thr) {
+        status = kConverged;
+        break;
+      }
+    }
+    if (status == kMaxIter && !std::isfinite(res)) status = kNonfinite;
+    std::memcpy(x_out + (size_t)s * n, x.data(), sizeof(double) * n);
+    iters[s] = iter;
+    conv[s] = (status == kConverged || status == kZeroRhs || status == kInitialOk) ? 1 : -1;
+    res_out[s] = res;
+    if (status_out) status_out[s] = status;
+    if (true_res) {
+      const double tr = reduce([&](int i, double d) {
+        const double ri = bs[i] - fast_row<double>(rp, ci, As, i, x.data());
+        return std::fma(ri, ri, d);
+      });
+      true_res[s] = std::sqrt(tr);
+    }
+  }
+  return 0;
+}
+
 ORC_API void orc_true_residual(int n, int nnz, const int* rp, const int* ci, int nsys, const double* A,
                                const double* b, const double* x, double* out) {
 #pragma omp parallel for schedule(static)

@@ -116,13 +116,14 @@ def ilu0(rp, ci, vals, approach=1):
     return out
 
 
-def parilu0(rp, ci, vals, sweeps, init=None):
+def parilu0(rp, ci, vals, sweeps, init=None, fast=False):
+    """fast: the reciprocal-multiply sweep of BILU_REDUCE_FAST."""
     rp, ci = _ia(rp), _ia(ci)
     vals = np.ascontiguousarray(vals, np.float64)
     init = None if init is None else np.ascontiguousarray(init, np.float64)
     out = np.zeros_like(vals)
-    lib().orc_parilu0(len(rp) - 1, vals.shape[1], _i(rp), _i(ci), vals.shape[0], _d(vals), _d(init), int(sweeps),
-                      _d(out))
+    lib().orc_parilu0_ex(len(rp) - 1, vals.shape[1], _i(rp), _i(ci), vals.shape[0], _d(vals), _d(init), int(sweeps),
+                         _d(out), int(bool(fast)))
     return out
 
 
@@ -190,6 +191,35 @@ def bicgstab(rp, ci, A, b, prec=PREC_LU, lu=None, ail=None, aiu=None, dot=0, tol
                        int(dot), int(tol_mode), C.c_double(tol), int(max_iter), _d(x), _f(iters), _i(conv), _d(res),
                        _i(status))
     return {"x": x, "iters": iters, "conv": conv, "res": res, "status": status}
+
+
+def bicgstab_fast(rp, ci, A, b, nt, pv=1, ail=None, aiu=None, fp32=False, tol_mode=0, tol=1e-11, max_iter=500):
+    """BILU_REDUCE_FAST order of the register-resident solver with `nt` threads per system.  pv: 0 none,
+    1 ISAI of L and U (ail, aiu = (row_ptrs, col_idxs, values)), 2 general ISAI (ail).  fp32: ISAI values
+    rounded to float and applied in float.  Returns x, iters, conv, res, status, true_res."""
+    rp, ci = _ia(rp), _ia(ci)
+    A = np.ascontiguousarray(A, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    nsys, n = b.shape
+    out = {"x": np.zeros_like(b), "iters": np.zeros(nsys, np.float32), "conv": np.zeros(nsys, np.int32),
+           "res": np.zeros(nsys), "status": np.zeros(nsys, np.int32), "true_res": np.zeros(nsys)}
+    empty = (np.zeros(1, np.int32), np.zeros(1, np.int32), None)
+    tri = []
+    for m in (ail, aiu):
+        if m is None:
+            tri.append((empty[0], empty[1], 0, None, None))
+            continue
+        vd = np.ascontiguousarray(m[2], np.float64)
+        vf = np.ascontiguousarray(m[2], np.float32) if fp32 else None
+        tri.append((_ia(m[0]), _ia(m[1]), len(m[1]), None if fp32 else vd, vf))
+    (lr, lc, ln, ld, lf), (ur, uc, un, ud, uf) = tri
+    rc = lib().orc_bicgstab_fast(n, A.shape[1], _i(rp), _i(ci), nsys, _d(A), _d(b), int(pv), int(bool(fp32)),
+                                 _i(lr), _i(lc), ln, _d(ld), _f(lf), _i(ur), _i(uc), un, _d(ud), _f(uf), int(nt),
+                                 int(tol_mode), C.c_double(tol), int(max_iter), _d(out["x"]), _f(out["iters"]),
+                                 _i(out["conv"]), _d(out["res"]), _i(out["status"]), _d(out["true_res"]))
+    if rc != 0:
+        raise ValueError("orc_bicgstab_fast: threads must be a multiple of 32 with at most 8 rows per thread")
+    return out
 
 
 def true_residual(rp, ci, A, b, x):

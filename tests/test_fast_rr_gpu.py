@@ -1,0 +1,110 @@
+"""The register-resident FAST solver (csrc/k_solve_rr.cu) against the oracle's
+restatement of its reduction order (orc_bicgstab_fast), bit for bit: ISAI of
+L and U (exact ILU or FAST ParILU factors), general ISAI and no
+preconditioner; FP64 and FP32 ISAI values; several threads-per-system
+choices (1 to 8 rows per thread); edge cases with their status words."""
+import numpy as np
+import pytest
+
+import bilu
+import helpers as H
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+NSYS = 10
+TOL = dict(tol_mode=bilu.TOL_REL, tol=1e-10)
+
+
+def _oracle_fast(rp, ci, v, b, precond, nt, fp32, approach=3, sweeps=5, power=2, **tol):
+    nrp, nci, src = O.add_missing_diag(rp, ci)
+    fv = np.where(src[None, :] >= 0, v[:, np.maximum(src, 0)], 0.0)
+    if precond == bilu.PRECOND_NONE:
+        return O.bicgstab_fast(rp, ci, v, b, nt, pv=0, **tol)
+    if precond == bilu.PRECOND_GENERAL_ISAI:
+        arp, aci = O.isai_pattern(nrp, nci, power)
+        ai = O.isai_values(nrp, nci, fv, 2, arp, aci)
+        return O.bicgstab_fast(rp, ci, v, b, nt, pv=2, ail=(arp, aci, ai), fp32=fp32, **tol)
+    if precond == bilu.PRECOND_ILU0_ISAI:
+        lu = O.ilu0(nrp, nci, fv, approach)
+    else:
+        lu = O.parilu0(nrp, nci, fv, sweeps, fast=True)
+    lrp, lci, urp, uci = O.split_pattern(nrp, nci)
+    Lv, Uv = O.split_values(nrp, nci, lu)
+    arp, aci = O.isai_pattern(lrp, lci, power)
+    brp, bci = O.isai_pattern(urp, uci, power)
+    ail = O.isai_values(lrp, lci, Lv, 0, arp, aci)
+    aiu = O.isai_values(urp, uci, Uv, 1, brp, bci)
+    return O.bicgstab_fast(rp, ci, v, b, nt, pv=1, ail=(arp, aci, ail), aiu=(brp, bci, aiu), fp32=fp32, **tol)
+
+
+def _check(g, o, what, fields=("iters", "conv", "status", "res", "x", "true_res")):
+    assert g["info"]["solver_kernel"] == 1, f"{what}: the register-resident kernel was not selected"
+    for f in fields:
+        H.assert_bitwise(g[f], o[f], f"{what}: {f}")
+
+
+CASES = [
+    ("2d5_16x16", bilu.PRECOND_ILU0_ISAI, dict(ilu_approach=3)),
+    ("3d7_7x7x7", bilu.PRECOND_PARILU0_ISAI, dict(parilu_sweeps=5)),
+    ("cd2d_12x12", bilu.PRECOND_GENERAL_ISAI, dict(isai_power=1)),
+    ("3d7_5x5x5", bilu.PRECOND_GENERAL_ISAI, dict(isai_power=2)),
+    ("2d5_8x8", bilu.PRECOND_NONE, {}),
+]
+
+
+@pytest.mark.parametrize("fam,precond,kw", CASES, ids=[f"{c[0]}-p{c[1]}" for c in CASES])
+@pytest.mark.parametrize("fp32", [False, True])
+@pytest.mark.parametrize("nt", [0, 64, 128])
+def test_rr_solver_bitwise(cuda, fam, precond, kw, fp32, nt):
+    if precond == bilu.PRECOND_NONE and fp32:
+        pytest.skip("no preconditioner values to round")
+    rp, ci, v, b = H.workload(fam, NSYS)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, reduction=bilu.REDUCE_FAST,
+                    factor_precision=bilu.FP32 if fp32 else bilu.FP64, threads_per_system=nt, **kw, **TOL)
+    used = g["info"]["threads"]
+    if nt:
+        assert used == nt
+    o = _oracle_fast(rp, ci, v, b, precond, used, fp32, approach=kw.get("ilu_approach", 3),
+                     sweeps=kw.get("parilu_sweeps", 5), power=kw.get("isai_power", 2), **TOL)
+    _check(g, o, f"{fam} precond {precond} fp32={fp32} threads={used}")
+    assert np.all(g["conv"] == 1)
+
+
+def test_rr_large_system_eight_rows_per_thread(cuda):
+    """n = 1000 (the benchmark's 3D 10x10x10 pattern): 128 threads, 8 rows each, FP32 ISAI."""
+    rp, ci, v, b = bilu.gen_stencil(2, 10, 10, 10, 6, seed=11)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_PARILU0_ISAI, parilu_sweeps=5,
+                    reduction=bilu.REDUCE_FAST, factor_precision=bilu.FP32, **TOL)
+    assert g["info"]["threads"] == 128
+    o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_PARILU0_ISAI, 128, True, **TOL)
+    _check(g, o, "3D 10x10x10 ParILU+ISAI FP32")
+
+
+def test_rr_edge_cases(cuda):
+    """Zero right-hand side, one already below the threshold, an iteration limit and a NaN in A."""
+    rp, ci, v, b = H.workload("2d5_8x8", 6)
+    b = b.copy()
+    v = v.copy()
+    b[1] = 0.0
+    b[2] *= 1e-14           # below the absolute threshold from the start
+    v[4, 3] = np.nan        # non-finite recurrences
+    for max_iter in (500, 2):
+        kw = dict(tol_mode=bilu.TOL_ABS, tol=1e-11, max_iter=max_iter)
+        g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0_ISAI, ilu_approach=3,
+                        reduction=bilu.REDUCE_FAST, **kw)
+        o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_ILU0_ISAI, g["info"]["threads"], False, **kw)
+        _check(g, o, f"edge cases, max_iter {max_iter}")
+        assert g["status"][1] == 2 and g["status"][2] == 3 and g["status"][4] == -3
+        if max_iter == 2:
+            assert g["status"][0] == -1
+
+
+def test_rr_matches_reference_order_in_iterations(cuda):
+    """Same method as the reference-order kernel: iteration counts within one of it."""
+    rp, ci, v, b = H.workload("3d7_7x7x7", NSYS)
+    ref = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0_ISAI, ilu_approach=3, **TOL)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0_ISAI, ilu_approach=3,
+                    reduction=bilu.REDUCE_FAST, **TOL)
+    assert ref["info"]["solver_kernel"] == 0 and g["info"]["solver_kernel"] == 1
+    assert np.all(np.abs(g["iters"] - ref["iters"]) <= 1.0)
+    np.testing.assert_allclose(g["x"], ref["x"], rtol=0, atol=1e-8 * np.abs(ref["x"]).max())
