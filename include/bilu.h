@@ -103,6 +103,10 @@ typedef struct bilu_options {
                                 triangular matrix itself and aiL divides by them, as
                                 GenerateISAI_gpu(lower_tri) (isai_gpu.cu:325-355) does for a
                                 stand-alone lower triangular matrix.  Solves reject 1.     */
+  int    smem_staging;       /* register-resident solver only: -1 automatic; else a bit mask
+                                of the operands copied to shared memory once per system
+                                (bit 0: A, bit 1: aiL / aiA, bit 2: aiU), the rest read
+                                through L1.  Operands that do not fit are left out.       */
 } bilu_options;
 
 /* Fills *opts with the reference defaults: merged ILU(0), approach 1, 5 sweeps,
@@ -199,6 +203,15 @@ typedef struct bilu_timing {
 } bilu_timing;
 bilu_status bilu_plan_enable_timing(bilu_plan* plan, int enable);
 bilu_status bilu_plan_last_timing(bilu_plan* plan, bilu_timing* timing);
+
+/* Times the register-resident solver's configurations on this batch -- threads
+ * per system 1x, 2x and 4x the fewest that give 8 rows per thread, shared-memory
+ * staging of none / aiL / aiL + aiU / A -- and keeps the fastest for the plan's
+ * later solves.  Plans that do not use that solver (bilu_plan_info.solver_kernel
+ * 0) are left unchanged.  Runs full solves of the batch (d_x is overwritten) and
+ * synchronises.  No reference counterpart. */
+bilu_status bilu_plan_autotune(bilu_plan* plan, int nsys, const double* d_values, const double* d_b,
+                               double* d_x, void* stream);
 
 /* bilu_solve without any device allocation.  No counterpart in the reference
  * (its solvers cudaMalloc and cudaFree their temporaries on every call).

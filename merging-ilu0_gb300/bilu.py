@@ -31,7 +31,7 @@ EXPORTED = [
     "bilu_plan_get_pattern", "bilu_expand_values", "bilu_solve", "bilu_solve_warm", "bilu_ilu0",
     "bilu_parilu0", "bilu_split_lu", "bilu_isai", "bilu_true_residual", "bilu_last_error",
     "bilu_version", "bilu_device_count", "bilu_gen_stencil", "bilu_gen_uneven", "bilu_plan_enable_timing",
-    "bilu_plan_last_timing", "bilu_solve_noalloc", "bilu_uneven_plan_create", "bilu_uneven_plan_destroy",
+    "bilu_plan_last_timing", "bilu_plan_autotune", "bilu_solve_noalloc", "bilu_uneven_plan_create", "bilu_uneven_plan_destroy",
     "bilu_uneven_autotune", "bilu_uneven_solve", "bilu_uneven_get_info", "bilu_forward_error",
     "bilu_mlp_create", "bilu_mlp_destroy", "bilu_mlp_param_count", "bilu_mlp_get_params", "bilu_mlp_set_params",
     "bilu_mlp_train", "bilu_mlp_loss_grad", "bilu_mlp_eval", "bilu_mlp_warm_start", "bilu_mlp_save", "bilu_mlp_load",
@@ -45,6 +45,7 @@ class Options(C.Structure):
         ("reduction", C.c_int), ("compute_true_residual", C.c_int), ("threads_per_system", C.c_int),
         ("parilu_res_tol", C.c_double),
         ("isai_lower_diag", C.c_int),
+        ("smem_staging", C.c_int),
     ]
 
 
@@ -313,6 +314,12 @@ class Plan:
 
     def enable_timing(self, enable=True):
         _check(lib().bilu_plan_enable_timing(self.h, 1 if enable else 0))
+
+    def autotune(self, values, b, x, stream=None):
+        """Keeps the fastest register-resident solver configuration for this batch (x is overwritten)."""
+        nsys = b.shape[0] if b.dim() > 1 else b.numel() // self.n
+        _check(lib().bilu_plan_autotune(self.h, nsys, _dev(values), _dev(b), _dev(x), _stream(stream)))
+        return self.info()
 
     def last_timing(self):
         t = Timing()

@@ -274,21 +274,18 @@ void choose_layout(bilu_plan& P) {
 }
 
 // Register-resident FAST solver: FAST order, ISAI or no preconditioner, at most
-// 8 rows per thread.  Threads per system: the caller's, else the fewest warps
-// that give every thread at most 8 rows (one warp for n <= 256).  Shared memory
-// beyond the mandatory part (reductions, SpMV input, preconditioner scratch)
-// holds A, then aiL, then aiU, while the CTA still fits as many times per SM
-// as its registers and threads allow.
-void choose_rr(bilu_plan& P) {
+// 8 rows per thread.  rr_configure sets the plan up for `nt` threads per system
+// and the shared-memory staging `mask` (bit 0 A, bit 1 aiL / aiA, bit 2 aiU;
+// operands that would cost occupancy are left in global memory, read through
+// L1); false when the kernel does not apply or that configuration is invalid.
+bool rr_configure(bilu_plan& P, int nt, int mask) {
   const bilu_options& o = P.opts;
-  P.rr = false;
   const int pk = prec_kind(o.precond);
-  if (o.reduction != BILU_REDUCE_FAST || (pk != PK_ISAI && pk != PK_NONE)) return;
+  if (o.reduction != BILU_REDUCE_FAST || (pk != PK_ISAI && pk != PK_NONE)) return false;
   const int n = P.n;
-  int nt = o.threads_per_system > 0 ? round_up(o.threads_per_system, 32) : round_up((n + 7) / 8, 32);
-  nt = std::max(nt, 32);
+  nt = std::max(round_up(nt, 32), 32);
   const int R = rr_rows_per_thread(n, nt);
-  if (R == 0 || nt > rr_max_threads(R)) return;
+  if (R == 0 || nt > rr_max_threads(R)) return false;
   const int pv = pk == PK_NONE ? 0 : (P.general_isai ? 2 : 1);
   const bool fp32 = is_fp32(o);
   const int fts = fp32 ? 4 : 8;
@@ -311,21 +308,35 @@ void choose_rr(bilu_plan& P) {
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(optin, off)) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, nt, off) != cudaSuccess || occ < 1) {
     cudaGetLastError();
-    return;
+    return false;
   }
   const int budget = std::min(optin, per_sm / occ - reserved);
-  if (off > budget) return;
-  auto stage = [&](int& dst, long long bytes) {
-    if (bytes > 0 && off + bytes <= budget) take(dst, bytes);
+  if (off > budget) return false;
+  auto stage = [&](int& dst, long long bytes, int bit) {
+    if ((mask & bit) && bytes > 0 && off + bytes <= budget) take(dst, bytes);
   };
-  stage(L.A, (long long)P.nnz_in * 8);
-  if (pv != 0) stage(L.ail, (long long)P.ail_rp[n] * fts);
-  if (pv == 1) stage(L.aiu, (long long)P.aiu_rp[n] * fts);
+  stage(L.A, (long long)P.nnz_in * 8, 1);
+  if (pv != 0) stage(L.ail, (long long)P.ail_rp[n] * fts, 2);
+  if (pv == 1) stage(L.aiu, (long long)P.aiu_rp[n] * fts, 4);
   L.total = off;
   P.rr = true;
   P.rr_threads = nt;
   P.rr_pv = pv;
   P.rr_lay = L;
+  return true;
+}
+
+// Default: the caller's threads per system, else the fewest warps that give
+// every thread at most 8 rows (one warp for n <= 256); the caller's staging
+// mask, else the ISAI values but not A.  Measured on GB300 (3D 7-point
+// 10x10x10, 7x7x7, 2D 16x16): A read through L1 beats A in shared memory, whose
+// carve-out shrinks the L1 left for the column indices and ISAI values; the
+// FP32 aiL in shared memory helps when it fits.
+void choose_rr(bilu_plan& P) {
+  const bilu_options& o = P.opts;
+  P.rr = false;
+  const int nt = o.threads_per_system > 0 ? o.threads_per_system : round_up((P.n + 7) / 8, 32);
+  rr_configure(P, nt, o.smem_staging >= 0 ? o.smem_staging : 6);
 }
 
 bilu_status upload(bilu_plan& P) {
@@ -449,8 +460,12 @@ bilu_status check_opts(const bilu_options* o) {
     return set_error(BILU_ERR_INVALID, "options: threads_per_system must be 0..1024");
   if (!(o->parilu_res_tol >= 0.0)) return set_error(BILU_ERR_INVALID, "options: parilu_res_tol must be >= 0");
   if (o->isai_lower_diag != 0 && o->isai_lower_diag != 1) return set_error(BILU_ERR_INVALID, "options: isai_lower_diag");
+  if (o->smem_staging < -1 || o->smem_staging > 7) return set_error(BILU_ERR_INVALID, "options: smem_staging must be -1..7");
   return BILU_OK;
 }
+
+bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double* lu_init, const double* b, double* x,
+                       const bilu_results* R, cudaStream_t st);
 
 }  // namespace plan_detail
 
@@ -476,6 +491,7 @@ void bilu_default_options(bilu_options* o) {
   o->threads_per_system = 0;
   o->parilu_res_tol = 0.0;
   o->isai_lower_diag = 0;
+  o->smem_staging = -1;
 }
 
 const char* bilu_last_error(void) { return g_last_error.c_str(); }
@@ -634,6 +650,50 @@ bilu_status bilu_plan_last_timing(bilu_plan* P, bilu_timing* t) {
   cudaEventElapsedTime(&t->solve_ms, P->ev[1], P->ev[2]);
   cudaEventElapsedTime(&t->total_ms, P->ev[0], P->ev[2]);
   return BILU_OK;
+}
+
+bilu_status bilu_plan_autotune(bilu_plan* P, int nsys, const double* d_values, const double* d_b, double* d_x,
+                               void* stream) {
+  if (!P) return set_error(BILU_ERR_INVALID, "bilu_plan_autotune: NULL plan");
+  if (nsys <= 0 || !d_values || !d_b || !d_x) return set_error(BILU_ERR_INVALID, "bilu_plan_autotune: bad arguments");
+  if (!P->rr) return BILU_OK;  // only the register-resident solver has choices
+  const bool had_timing = P->timing;
+  bilu_status st = bilu_plan_enable_timing(P, 1);
+  if (st) return st;
+  const int base = round_up((P->n + 7) / 8, 32);
+  const int keep_nt = P->rr_threads;
+  const RRLayout keep_lay = P->rr_lay;
+  float best = -1.0f;
+  int best_nt = keep_nt, best_mask = -1;
+  for (int f : {1, 2, 4}) {
+    for (int mask : {0, 2, 6, 1}) {
+      if (!rr_configure(*P, base * f, mask)) continue;
+      float ms = 0.0f;
+      for (int rep = 0; rep < 2; ++rep) {  // the first run warms caches; the second is timed
+        st = solve_impl(P, nsys, d_values, nullptr, d_b, d_x, nullptr, (cudaStream_t)stream);
+        if (st) break;
+        bilu_timing t;
+        st = bilu_plan_last_timing(P, &t);
+        if (st) break;
+        ms = t.solve_ms;
+      }
+      if (st) break;
+      if (best < 0.0f || ms < best) {
+        best = ms;
+        best_nt = base * f;
+        best_mask = mask;
+      }
+    }
+    if (st) break;
+  }
+  if (best_mask >= 0) {
+    rr_configure(*P, best_nt, best_mask);
+  } else {
+    P->rr_threads = keep_nt;
+    P->rr_lay = keep_lay;
+  }
+  P->timing = had_timing;
+  return st;
 }
 
 bilu_status bilu_plan_destroy(bilu_plan* P) {

@@ -69,18 +69,36 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* red, int nw) {
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 
-template <typename VT, typename XT>
-__device__ __forceinline__ XT row_acc(const VT* __restrict__ val, const int* __restrict__ ci, int beg, int end,
-                                      const XT* __restrict__ xv) {
-  XT acc = XT(0);
-  for (int k = beg; k < end; ++k) acc = fma_t((XT)val[k], xv[__ldg(ci + k)], acc);
-  return acc;
+// out[k] = row (tid + k*nt) of M times xv, for the R rows of this thread
+// (rows >= n give 0).  The R rows advance together, entry j of every row per
+// step, so the thread has R independent FMA chains in flight (64-cycle FP64
+// latency) instead of one; each row still sums its entries in ascending order
+// from 0.
+template <int R, typename VT, typename XT>
+__device__ __forceinline__ void rows_acc(const VT* __restrict__ val, const int* __restrict__ ci,
+                                         const int* __restrict__ rp, int tid, int nt, int n,
+                                         const XT* __restrict__ xv, XT (&out)[R]) {
+  int beg[R], len[R];
+  int jmax = 0;
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int i = tid + k * nt;
+    beg[k] = i < n ? __ldg(rp + i) : 0;
+    len[k] = i < n ? __ldg(rp + i + 1) - beg[k] : 0;
+    jmax = max(jmax, len[k]);
+    out[k] = XT(0);
+  }
+  for (int j = 0; j < jmax; ++j) {
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+      if (j < len[k]) out[k] = fma_t((XT)val[beg[k] + j], xv[__ldg(ci + beg[k] + j)], out[k]);
+  }
 }
 
 // PV: 0 none, 1 ISAI of L and U (z = aiU (aiL v)), 2 general ISAI (z = aiA v).
 // FT: type of the ISAI values and of the preconditioner arithmetic.
 template <int R, int PV, typename FT>
-__global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : 256), 1)
+__global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 : 128)), R == 8 ? 3 : 1)
     k_bicgstab_rr(const SolveArgs a, const RRLayout L) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int sys = blockIdx.x;
@@ -164,20 +182,25 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : 256), 1)
 #define BILU_RR_APPLY()                                                                                          \
   do {                                                                                                           \
     if (PV == 1) {                                                                                               \
+      FT z_[R];                                                                                                  \
+      rows_acc<R>(AIL, P.ail_ci, P.ail_rp, tid, nt, n, sin, z_);                                                 \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
         const int i = tid + k * nt;                                                                              \
-        if (i < n) smid[i] = row_acc(AIL, P.ail_ci, __ldg(P.ail_rp + i), __ldg(P.ail_rp + i + 1), sin);          \
+        if (i < n) smid[i] = z_[k];                                                                              \
       }                                                                                                          \
       __syncthreads();                                                                                           \
+      rows_acc<R>(AIU, P.aiu_ci, P.aiu_rp, tid, nt, n, smid, z_);                                                \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
         const int i = tid + k * nt;                                                                              \
-        if (i < n) sph[i] = (double)row_acc(AIU, P.aiu_ci, __ldg(P.aiu_rp + i), __ldg(P.aiu_rp + i + 1), smid); \
+        if (i < n) sph[i] = (double)z_[k];                                                                       \
       }                                                                                                          \
       __syncthreads();                                                                                           \
     } else if (PV == 2) {                                                                                        \
+      FT z_[R];                                                                                                  \
+      rows_acc<R>(AIL, P.ail_ci, P.ail_rp, tid, nt, n, sin, z_);                                                 \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
         const int i = tid + k * nt;                                                                              \
-        if (i < n) sph[i] = (double)row_acc(AIL, P.ail_ci, __ldg(P.ail_rp + i), __ldg(P.ail_rp + i + 1), sin);   \
+        if (i < n) sph[i] = (double)z_[k];                                                                       \
       }                                                                                                          \
       __syncthreads();                                                                                           \
     }                                                                                                            \
@@ -209,14 +232,12 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : 256), 1)
     __syncthreads();
     BILU_RR_APPLY();  // p_hat in sph
     // v = A p_hat, (r_hat, v)
+    rows_acc<R>(Am, aci, arp, tid, nt, n, sph, v);
     q[0] = 0.0;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       const int i = tid + k * nt;
-      if (i < n) {
-        v[k] = row_acc(Am, aci, __ldg(arp + i), __ldg(arp + i + 1), sph);
-        q[0] = fma(__ldg(bg + i), v[k], q[0]);
-      }
+      if (i < n) q[0] = fma(__ldg(bg + i), v[k], q[0]);
     }
     block_sum<1>(q, red + 64, nw);
     alpha = rho / q[0];
@@ -243,12 +264,12 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : 256), 1)
     }
     BILU_RR_APPLY();  // s_hat in sph
     // t = A s_hat, (t, s), (t, t)
+    rows_acc<R>(Am, aci, arp, tid, nt, n, sph, t);
     double q2[2] = {0.0, 0.0};
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       const int i = tid + k * nt;
       if (i < n) {
-        t[k] = row_acc(Am, aci, __ldg(arp + i), __ldg(arp + i + 1), sph);
         q2[0] = fma(t[k], r[k], q2[0]);
         q2[1] = fma(t[k], t[k], q2[1]);
       }
@@ -307,12 +328,14 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : 256), 1)
       if (i < n) sph[i] = x[k];
     }
     __syncthreads();
+    double ax[R];
+    rows_acc<R>(Am, aci, arp, tid, nt, n, sph, ax);
     q[0] = 0.0;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       const int i = tid + k * nt;
       if (i < n) {
-        const double ri = __ldg(bg + i) - row_acc(Am, aci, __ldg(arp + i), __ldg(arp + i + 1), sph);
+        const double ri = __ldg(bg + i) - ax[k];
         q[0] = fma(ri, ri, q[0]);
       }
     }
@@ -358,7 +381,7 @@ int rr_rows_per_thread(int n, int nt) {
   return 0;
 }
 
-int rr_max_threads(int R) { return R <= 1 ? 1024 : (R == 2 ? 512 : 256); }
+int rr_max_threads(int R) { return R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 : 128)); }
 
 const void* rr_kernel(int pv, int fp32, int R) {
   if (pv == 0) return rr_kernel_pv<0, double>(R);

@@ -91,7 +91,8 @@ bool same_options(const bilu_options& a, const bilu_options& b) {
          a.isai_power == b.isai_power && a.tol_mode == b.tol_mode && a.tol == b.tol && a.max_iter == b.max_iter &&
          a.factor_precision == b.factor_precision && a.reduction == b.reduction &&
          a.compute_true_residual == b.compute_true_residual && a.threads_per_system == b.threads_per_system &&
-         a.parilu_res_tol == b.parilu_res_tol && a.isai_lower_diag == b.isai_lower_diag;
+         a.parilu_res_tol == b.parilu_res_tol && a.isai_lower_diag == b.isai_lower_diag &&
+         a.smem_staging == b.smem_staging;
 }
 
 class PlanCache {

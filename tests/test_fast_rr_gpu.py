@@ -108,3 +108,21 @@ def test_rr_matches_reference_order_in_iterations(cuda):
     assert ref["info"]["solver_kernel"] == 0 and g["info"]["solver_kernel"] == 1
     assert np.all(np.abs(g["iters"] - ref["iters"]) <= 1.0)
     np.testing.assert_allclose(g["x"], ref["x"], rtol=0, atol=1e-8 * np.abs(ref["x"]).max())
+
+
+def test_rr_autotuned_plan_bitwise(cuda):
+    """bilu_plan_autotune picks threads per system and shared-memory staging; the solves that follow
+    still equal the oracle's order for the chosen thread count."""
+    import torch
+    rp, ci, v, b = H.workload("3d7_7x7x7", 64)
+    opts = dict(precond=bilu.PRECOND_PARILU0_ISAI, parilu_sweeps=5, reduction=bilu.REDUCE_FAST,
+                factor_precision=bilu.FP32, **TOL)
+    with bilu.Plan(rp, ci, **opts) as plan:
+        V = torch.from_numpy(v).to(cuda)
+        B = torch.from_numpy(b).to(cuda)
+        X = torch.empty_like(B)
+        info = plan.autotune(V, B, X)
+        assert info["solver_kernel"] == 1 and info["threads"] in (64, 128, 256)
+    g = H.gpu_solve(cuda, rp, ci, v, b, threads_per_system=info["threads"], **opts)
+    o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_PARILU0_ISAI, info["threads"], True, **TOL)
+    _check(g, o, f"autotuned threads {info['threads']}")
