@@ -34,18 +34,29 @@ SEED = 20261203
 METRIC = "systems solved/sec at rel. residual 1e-10: chosen vs plain form, % HBM roofline"
 
 # workloads: (kind, gx, gy, gz, nsys, options)
-HEADLINE = dict(name="parilu5_isai_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096,
-                desc="ParILU(0) 5 sweeps + ISAI(L,U on |T|^2) BiCGSTAB, 4096 FP64 systems, 3D 7-point 10x10x10 "
-                     "(n=1000, nnz=6400), Peclet skew U(0,0.5), rel. tol 1e-10, max 500 iterations",
+HEADLINE = dict(name="parilu5_isai_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096, autotune=True,
+                desc="ParILU(0) 5 sweeps + ISAI(L,U on |T|^2) BiCGSTAB, ISAI stored and applied in FP32 (A*x, inner "
+                     "products, recurrences, ParILU in FP64), 4096 FP64 systems, 3D 7-point 10x10x10 (n=1000, "
+                     "nnz=6400), Peclet skew U(0,0.5), rel. tol 1e-10, max 500 iterations",
                 opts=dict(precond=4, parilu_sweeps=5, isai_power=2, tol_mode=1, tol=1e-10, max_iter=500,
-                          reduction=1, factor_precision=0), fwd_sample=32)
+                          reduction=1, factor_precision=1), fwd_sample=32)
 SECONDARY = [
+    dict(name="parilu5_isai_3d7_10x10x10_fp64", kind=2, grid=(10, 10, 10), nsys=4096, autotune=True,
+         desc="headline workload with FP64 ISAI values",
+         opts=dict(precond=4, parilu_sweeps=5, isai_power=2, tol_mode=1, tol=1e-10, reduction=1, factor_precision=0)),
+    dict(name="plain_ilu0_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096,
+         desc="plain form on the headline systems: merged FP64 ILU(0) BiCGSTAB (shared-memory kernel), FAST order",
+         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1)),
     dict(name="plain_ilu0_2d5_16x16_fast", kind=1, grid=(16, 16, 1), nsys=16384,
          desc="plain form: merged ILU(0) BiCGSTAB, 16384 FP64 systems, 2D 5-point 16x16, rel 1e-10, FAST order",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1)),
     dict(name="plain_ilu0_2d5_16x16_ref", kind=1, grid=(16, 16, 1), nsys=16384,
          desc="plain form in the reference's operation order (bit-identical iterates)",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=0)),
+    dict(name="fp32_isai_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768, autotune=True,
+         desc="ILU(0) + ISAI stored and applied in FP32 (FP64 A*x, inner products, recurrences), 32768 "
+              "convection-diffusion systems 24x24",
+         opts=dict(precond=3, ilu_approach=3, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1), fwd_sample=256),
     dict(name="fp32_ilu0_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768,
          desc="FP32-stored ILU(0) factors (FP64 recurrences), 32768 convection-diffusion systems 24x24",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1), fwd_sample=256),
@@ -179,6 +190,8 @@ def measure(wl, steps, warmup, dev, stream, sampler=None, e2e=False, timed_hook=
     st = torch.empty(nsys, dtype=torch.int32, device=dev)
     del v, b
     with torch.cuda.stream(stream):
+        if wl.get("autotune"):
+            plan.autotune(V, B, X, stream=stream)  # configuration search, outside the timed region
         for _ in range(warmup):
             plan.solve(V, B, X, it, cv, rs, tr, st, stream=stream)
         torch.cuda.synchronize()
@@ -293,12 +306,12 @@ def measure_uneven(dev, stream, nsys=8192, steps=3, warmup=2):
 def measure_learned(dev, stream, ntrain=65536, neval=16384, train_steps=1500, batch=65536, steps=3):
     """Learned ParILU warm start on 3D 7-point 7x7x7 systems: train the MLP on the converged ParILU(0)
     factors of `ntrain` systems, then solve `neval` fresh systems with ParILU sweeps until the ILU residual is
-    <= 1e-6 (at most 40) + BiCGSTAB (FP32 factors, FAST order, rel 1e-10), with the plain A-value start and
+    <= 1e-6 (at most 40) + ISAI in FP32 + BiCGSTAB (FAST order, rel 1e-10), with the plain A-value start and
     with the learned warm start (fallback to A values when its ILU residual exceeds 1e-3)."""
     import torch
     import bilu
     rp, ci, v, _ = bilu.gen_stencil(5, 7, 7, 7, ntrain, SEED + 1)
-    opts = dict(precond=2, parilu_sweeps=40, parilu_res_tol=1e-6, tol_mode=1, tol=1e-10, reduction=1,
+    opts = dict(precond=4, parilu_sweeps=40, parilu_res_tol=1e-6, tol_mode=1, tol=1e-10, reduction=1,
                 factor_precision=1)
     plan = bilu.Plan(rp, ci, **opts)
     V = torch.from_numpy(v).to(dev)
@@ -321,6 +334,8 @@ def measure_learned(dev, stream, ntrain=65536, neval=16384, train_steps=1500, ba
     LU0 = torch.empty_like(V2)
     res = torch.empty(neval, dtype=torch.float64, device=dev)
     used = torch.empty(neval, dtype=torch.int32, device=dev)
+    with torch.cuda.stream(stream):
+        plan.autotune(V2, B2, X, stream=stream)
     out = {"name": "learned_warm_start_3d7_7x7x7", "ntrain": ntrain, "neval": neval, "train_steps": train_steps,
            "batch": batch, "train_s": train_s, "loss_first": float(losses[:10].mean()),
            "loss_last": float(losses[-10:].mean())}
@@ -367,7 +382,7 @@ def measure_learned(dev, stream, ntrain=65536, neval=16384, train_steps=1500, ba
                                                 out["plain_ilu0_fp64"]["systems_per_s"])
     out["workload"] = ("learned ParILU warm start: MLP 9-64-64-1 (GELU, BF16 weights, FP32 accumulation) trained on "
                        "65536 3D 7-point 7x7x7 systems' converged ParILU(0) factors; 16384 fresh systems, ParILU "
-                       "sweeps to ILU residual 1e-6 + BiCGSTAB with FP32 factors, rel 1e-10")
+                       "sweeps to ILU residual 1e-6 + ISAI(L,U) stored and applied in FP32 + BiCGSTAB, rel 1e-10")
     m.close()
     plan.close()
     return out
@@ -447,22 +462,30 @@ def main():
             secondary.append({"name": "learned_warm_start_3d7_7x7x7", "error": str(ex)})
     if rank != 0:
         return
-    chosen = None
+    chosen = {}
     for sc in secondary:
+        if sc.get("name") == "plain_ilu0_3d7_10x10x10" and "systems_per_s" in sc:
+            chosen["headline_3d7_10x10x10"] = {
+                "workload": HEADLINE["desc"], "plain_form": "merged FP64 ILU(0) + BiCGSTAB on the same systems",
+                "plain_systems_per_s": sc["systems_per_s"],
+                "chosen_form": "ParILU(5) + ISAI stored and applied in FP32, register-resident solver",
+                "chosen_systems_per_s": res["systems_per_s"], "ratio": res["systems_per_s"] / sc["systems_per_s"]}
         if sc.get("name") == "learned_warm_start_3d7_7x7x7" and "learned" in sc:
-            chosen = {"workload": "16384 fresh 3D 7-point 7x7x7 systems (n=343), rel. tol 1e-10",
-                      "plain_form": "merged FP64 ILU(0) + BiCGSTAB",
-                      "plain_systems_per_s": sc["plain_ilu0_fp64"]["systems_per_s"],
-                      "chosen_form": "learned warm start + ParILU sweeps to ILU residual 1e-6 + FP32-stored factors",
-                      "chosen_systems_per_s": sc["learned"]["systems_per_s"],
-                      "ratio": sc["speedup_chosen_vs_plain_ilu0_fp64"]}
+            chosen["learned_3d7_7x7x7"] = {
+                "workload": "16384 fresh 3D 7-point 7x7x7 systems (n=343), rel. tol 1e-10",
+                "plain_form": "merged FP64 ILU(0) + BiCGSTAB",
+                "plain_systems_per_s": sc["plain_ilu0_fp64"]["systems_per_s"],
+                "chosen_form": "learned warm start + ParILU sweeps to ILU residual 1e-6 + ISAI in FP32",
+                "chosen_systems_per_s": sc["learned"]["systems_per_s"],
+                "ratio": sc["speedup_chosen_vs_plain_ilu0_fp64"]}
     n, nnz, nsys = res["n"], res["nnz"], res["nsys"]
     info = res["info"]
     hbm, peak_kind = load_peaks()
     bps = bytes_per_system(n, nnz)
     solve_s = res["solve_ms"] / 1e3
     achieved = bps * nsys / solve_s / 1e9
-    prec_nnz = info["nnz_isai_L"] + info["nnz_isai_U"]
+    fp32_prec = HEADLINE["opts"].get("factor_precision", 0) == 1
+    prec_nnz = 0 if fp32_prec else info["nnz_isai_L"] + info["nnz_isai_U"]  # FP32 ISAI work is not FP64
     flops = fp64_flops_per_iter(n, nnz, prec_nnz, HEADLINE["opts"]["precond"]) * res["mean_iters"] * nsys
     fp64_peak = 1205.0  # GFLOP/s: 602.5 G DFMA/s measured on this machine's GB300 (full-warp DFMA stream)
     cores = os.cpu_count()
@@ -473,7 +496,8 @@ def main():
         "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": HEADLINE["desc"], "nsys": nsys, "n": n, "nnz": nnz, "reduction": "fast",
-                   "factor_precision": "fp64", "threads_per_system": info["threads"],
+                   "factor_precision": "fp32 ISAI (FP64 A*x, inner products, recurrences, ParILU)" if fp32_prec
+                   else "fp64", "threads_per_system": info["threads"], "solver_kernel": info["solver_kernel"],
                    "smem_bytes_per_system": info["smem_bytes"],
                    "l2": "inputs larger than L2: A values %.0f MB per step" % (nsys * nnz * 8 / 1e6),
                    "parallelism": f"weak: {world} independent batch(es), one per GPU"},
@@ -481,7 +505,7 @@ def main():
         "e2e": res["e2e"],
         "gpu_launches": 3 * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_bicgstab (solver)",
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_bicgstab_rr (register-resident solver)" if info["solver_kernel"] == 1 else "k_bicgstab (solver)",
                      "bytes_per_system": bps},
         "roofline_fp64": {"achieved": flops / solve_s / 1e9, "peak": fp64_peak, "unit": "GFLOP/s",
                           "frac": flops / solve_s / 1e9 / fp64_peak,
@@ -493,7 +517,7 @@ def main():
         "cpu_baseline": {"value": rate, "unit": "systems/s", "cores": used, "kind": "port",
                          "sample": f"{cpu_sample} systems of the headline workload through the CPU restatement "
                                    f"({dt:.2f} s, {used} OpenMP threads of {cores} host cores)"},
-        "chosen_vs_plain": chosen,
+        "chosen_vs_plain": chosen or None,
         "secondary": secondary,
     }
     print(json.dumps(line))

@@ -255,6 +255,9 @@ bilu_status bilu_split_lu(const bilu_plan* plan, int nsys, const double* d_lu,
  * For a BILU_PRECOND_GENERAL_ISAI plan: d_lu holds A's values (factor pattern),
  * d_ail receives the ISAI of A (GenerateISAI_gpu(aiA, A, general, p)) and
  * d_aiu is not used.
+ * With a BILU_REDUCE_FAST plan the aiU entries are multiplied by the correctly
+ * rounded reciprocal of the diagonal instead of divided by it, as the plan's
+ * solver does; BILU_REDUCE_REF keeps the reference's divisions.
  * Replaces GenerateISAI_gpu(aiL, L, lower_tri, p) and (aiU, U, upper_tri, p)
  * (isai.h:9, isai_gpu.cu:720). */
 bilu_status bilu_isai(const bilu_plan* plan, int nsys, const double* d_lu,

@@ -82,6 +82,11 @@ struct DevPattern {
   // entries without dependency pairs): the ones the learned warm start predicts
   int n_mlp = 0;
   const int* mlp_ent = nullptr;
+  // ParILU sweep order: entries with dependency pairs (most pairs first), then
+  // lower entries without pairs (l = a / u_jj), then upper entries without
+  // pairs (u = a); warps of one class do the same operations
+  const int* pl_ent = nullptr;  // nnz
+  int pl_ndep = 0, pl_nlow = 0;
 };
 
 // Shared-memory carve-up of the solver kernel for one system (byte offsets;
@@ -210,7 +215,7 @@ cudaError_t launch_parilu0(const DevPattern& p, int nsys, const double* A, const
                            int sweeps, int threads, cudaStream_t st, double res_tol = 0.0, int* sweeps_out = nullptr,
                            double* res_out = nullptr, int fast = 0);
 cudaError_t launch_isai(const DevPattern& p, int nsys, const double* lu, void* ail, void* aiu, int fp32,
-                        int threads, cudaStream_t st);
+                        int threads, cudaStream_t st, int fast = 0);
 cudaError_t launch_dense_solve(const DevPattern& p, int nsample, const int* sys_ids, const double* A, const double* b,
                                double* work, double* x_out, cudaStream_t st);
 cudaError_t launch_mlp_rowstats(const DevPattern& p, int nsys, const double* A, float* rown, float* coln, float* corr,
@@ -250,6 +255,8 @@ struct bilu_plan {
   std::vector<int> dep;  // pairs
   std::vector<int> l_rp, l_ci, l_src, u_rp, u_ci, u_src;
   std::vector<int> row_lev, tpos, mlp_ent;
+  std::vector<int> pl_ent;  // ParILU entry classes (see DevPattern::pl_ent)
+  int pl_ndep = 0, pl_nlow = 0;
   bool has_isai = false;
   std::vector<int> ail_rp, ail_ci, aiu_rp, aiu_ci;
   std::vector<int> ail_prog_ptr, ail_prog, aiu_prog_ptr, aiu_prog;  // prog in int units (pairs)

@@ -160,7 +160,8 @@ extern "C" bilu_status bilu_solve_noalloc(bilu_plan* P, int nsys, const double* 
     if (e != cudaSuccess) return cuda_fail(e, "factorisation");
     if (isai) {
       if (prec != BILU_PRECOND_GENERAL_ISAI) {
-        e = launch_isai(P->dp, nsys, lu, ws + off_ail, ws + off_aiu, fp32 ? 1 : 0, ft, s);
+        e = launch_isai(P->dp, nsys, lu, ws + off_ail, ws + off_aiu, fp32 ? 1 : 0, ft, s,
+                        o.reduction == BILU_REDUCE_FAST ? 1 : 0);
         if (e != cudaSuccess) return cuda_fail(e, "isai");
       }
       a.prec = PK_ISAI;

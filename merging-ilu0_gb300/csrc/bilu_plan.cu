@@ -355,6 +355,7 @@ bilu_status upload(bilu_plan& P) {
   const size_t o_dp = put(P.dep_ptr), o_dep = put(P.dep);
   const size_t o_lsrc = put(P.l_src), o_usrc = put(P.u_src);
   const size_t o_rlev = put(P.row_lev), o_tpos = put(P.tpos), o_ment = put(P.mlp_ent);
+  const size_t o_plent = put(P.pl_ent);
   size_t o_alrp = 0, o_alci = 0, o_aurp = 0, o_auci = 0, o_alpp = 0, o_alp = 0, o_aupp = 0, o_aup = 0;
   size_t o_gmp = 0, o_gm = 0, o_gp = 0;
   if (P.general_isai) {
@@ -408,6 +409,9 @@ bilu_status upload(bilu_plan& P) {
   d.tpos = b + o_tpos;
   d.n_mlp = (int)P.mlp_ent.size();
   d.mlp_ent = b + o_ment;
+  d.pl_ent = b + o_plent;
+  d.pl_ndep = P.pl_ndep;
+  d.pl_nlow = P.pl_nlow;
   if (P.has_isai) {
     d.ail_nnz = P.ail_rp[P.n];
     d.l_diag = P.opts.isai_lower_diag ? 1 : 0;
@@ -603,6 +607,24 @@ bilu_status bilu_plan_create(bilu_plan** out, int n, int nnz, const int* h_rp, c
       P->tpos[k] = find_pos(P->rp, P->ci, P->ci[k], i);
       if (P->ci[k] < i || P->dep_ptr[k + 1] > P->dep_ptr[k]) P->mlp_ent.push_back(k);
     }
+  {
+    std::vector<int> with_deps, lower, upper;
+    for (int i = 0; i < n; ++i)
+      for (int k = P->rp[i]; k < P->rp[i + 1]; ++k) {
+        if (P->dep_ptr[k + 1] > P->dep_ptr[k])
+          with_deps.push_back(k);
+        else
+          (P->ci[k] < i ? lower : upper).push_back(k);
+      }
+    std::stable_sort(with_deps.begin(), with_deps.end(), [&](int a, int b) {
+      return P->dep_ptr[a + 1] - P->dep_ptr[a] > P->dep_ptr[b + 1] - P->dep_ptr[b];
+    });
+    P->pl_ndep = (int)with_deps.size();
+    P->pl_nlow = (int)lower.size();
+    P->pl_ent = with_deps;
+    P->pl_ent.insert(P->pl_ent.end(), lower.begin(), lower.end());
+    P->pl_ent.insert(P->pl_ent.end(), upper.begin(), upper.end());
+  }
   P->has_isai = is_isai(P->opts.precond);
   P->general_isai = P->opts.precond == BILU_PRECOND_GENERAL_ISAI;
   if (P->has_isai) {
@@ -849,7 +871,7 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
     if (is_isai(prec)) {
       void* ail = ws + off_ail;
       void* aiu = ws + off_aiu;
-      e = launch_isai(P->dp, nsys, lu, ail, aiu, fp32 ? 1 : 0, ft, st);
+      e = launch_isai(P->dp, nsys, lu, ail, aiu, fp32 ? 1 : 0, ft, st, o.reduction == BILU_REDUCE_FAST ? 1 : 0);
       if (e != cudaSuccess) return cuda_err(e, "isai");
       a.prec = PK_ISAI;
       a.ail = ail;
@@ -949,7 +971,8 @@ bilu_status bilu_isai(const bilu_plan* P, int nsys, const double* d_lu, double* 
   if (!P->has_isai) return set_error(BILU_ERR_INVALID, "bilu_isai: plan was not created with an ISAI preconditioner");
   cudaError_t e = P->general_isai
                       ? launch_isai_general(P->dp, nsys, d_lu, d_ail, 0, fact_threads(P), (cudaStream_t)stream)
-                      : launch_isai(P->dp, nsys, d_lu, d_ail, d_aiu, 0, fact_threads(P), (cudaStream_t)stream);
+                      : launch_isai(P->dp, nsys, d_lu, d_ail, d_aiu, 0, fact_threads(P), (cudaStream_t)stream,
+                                    P->opts.reduction == BILU_REDUCE_FAST ? 1 : 0);
   return e == cudaSuccess ? BILU_OK : cuda_err(e, "isai");
 }
 

@@ -136,14 +136,17 @@ __global__ void __launch_bounds__(512) k_parilu0(const DevPattern P, int nsys, c
     const bool last = (it == sweeps);
     if (last && !track) break;
     if (FAST && !last) {
-      for (int r = threadIdx.x; r < P.n; r += blockDim.x) rinv[r] = 1.0 / cur[__ldg(P.diag + r)];
+      // __drcp_rn is the correctly rounded reciprocal, the same value as 1.0 / u
+      for (int r = threadIdx.x; r < P.n; r += blockDim.x) rinv[r] = __drcp_rn(cur[__ldg(P.diag + r)]);
       __syncthreads();
     }
-    for (int k = threadIdx.x; k < nnz; k += blockDim.x) {
+    // entries with dependency pairs (most pairs first, so a warp's lanes run alike)
+    for (int q = threadIdx.x; q < P.pl_ndep; q += blockDim.x) {
+      const int k = __ldg(P.pl_ent + q);
       const int pb = __ldg(P.dep_ptr + k), pe = __ldg(P.dep_ptr + k + 1);
       double s = 0.0;
-      for (int q = pb; q < pe; ++q) {
-        const int2 d = __ldg(P.dep + q);
+      for (int q2 = pb; q2 < pe; ++q2) {
+        const int2 d = __ldg(P.dep + q2);
         s = fma(cur[d.x], cur[d.y], s);
       }
       const int i = __ldg(P.row_of + k), j = __ldg(P.ci + k);
@@ -157,6 +160,25 @@ __global__ void __launch_bounds__(512) k_parilu0(const DevPattern P, int nsys, c
         if (j < i) v = FAST ? v * rinv[j] : v / cur[__ldg(P.diag + j)];
         nxt[k] = v;
       }
+    }
+    // lower entries without pairs: the sum is 0, so l = a / u_jj (a - 0 == a exactly)
+    const int lend = P.pl_ndep + P.pl_nlow;
+    for (int q = P.pl_ndep + threadIdx.x; q < lend; q += blockDim.x) {
+      const int k = __ldg(P.pl_ent + q), j = __ldg(P.ci + k);
+      if (track) {
+        const double r = As[k] - fma(cur[k], cur[__ldg(P.diag + j)], 0.0);
+        r2 = fma(r, r, r2);
+      }
+      if (!last) nxt[k] = FAST ? As[k] * rinv[j] : As[k] / cur[__ldg(P.diag + j)];
+    }
+    // upper entries without pairs: u = a, no arithmetic
+    for (int q = lend + threadIdx.x; q < nnz; q += blockDim.x) {
+      const int k = __ldg(P.pl_ent + q);
+      if (track) {
+        const double r = As[k] - (0.0 + cur[k]);
+        r2 = fma(r, r, r2);
+      }
+      if (!last) nxt[k] = As[k];
     }
     if (track) {
       const double tot = block_sum(r2, red);
@@ -189,7 +211,11 @@ __global__ void __launch_bounds__(512) k_parilu0(const DevPattern P, int nsys, c
 // The per-row program lists the structurally nonzero (c, position) pairs in
 // exactly that order (zeros of T(J,J) give exact no-op updates).  m is
 // accumulated in FP64 in shared memory and rounded to FT on the way out.
-template <typename FT>
+// FAST (BILU_REDUCE_FAST): the aiU entries are multiplied by the correctly
+// rounded reciprocal of the diagonal (__drcp_rn, one per row, the same value
+// as 1.0 / u) instead of divided -- one FP64 reciprocal per row instead of a
+// division per aiU entry.  The unit-diagonal aiL is unchanged.
+template <typename FT, bool FAST>
 __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, const double* __restrict__ LUg,
                                               FT* __restrict__ ail, FT* __restrict__ aiu) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -220,10 +246,15 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
   for (int k = threadIdx.x; k < P.ail_nnz; k += blockDim.x) ail[(size_t)sys * P.ail_nnz + k] = (FT)M[k];
   __syncthreads();
   // ---- aiU
+  double* rinv = M + (P.ail_nnz > P.aiu_nnz ? P.ail_nnz : P.aiu_nnz);  // FAST: n reciprocals
+  if (FAST) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) rinv[i] = __drcp_rn(LU[__ldg(P.diag + i)]);
+    __syncthreads();
+  }
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const int beg = __ldg(P.aiu_rp + i), sz = __ldg(P.aiu_rp + i + 1) - beg;
     double* m = M + beg;
-    m[0] = 1.0 / LU[__ldg(P.diag + i)];
+    m[0] = FAST ? rinv[i] : 1.0 / LU[__ldg(P.diag + i)];
     int q = __ldg(P.aiu_prog_ptr + i);
     for (int blk = 1; blk < sz; ++blk) {
       const int2 h = __ldg(P.aiu_prog + q++);
@@ -233,7 +264,7 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
         acc = fma(-m[e.x], LU[e.y], acc);
       }
       const int jt = __ldg(P.aiu_ci + beg + h.x);
-      m[h.x] = acc / LU[__ldg(P.diag + jt)];
+      m[h.x] = FAST ? acc * rinv[jt] : acc / LU[__ldg(P.diag + jt)];
     }
   }
   __syncthreads();
@@ -393,20 +424,15 @@ cudaError_t launch_parilu0(const DevPattern& p, int nsys, const double* A, const
 }
 
 cudaError_t launch_isai(const DevPattern& p, int nsys, const double* lu, void* ail, void* aiu, int fp32, int threads,
-                        cudaStream_t st) {
+                        cudaStream_t st, int fast) {
   if (nsys == 0) return cudaSuccess;
-  const int smem = (p.nnz + (p.ail_nnz > p.aiu_nnz ? p.ail_nnz : p.aiu_nnz)) * 8;
-  cudaError_t e;
-  if (fp32) {
-    e = cudaFuncSetAttribute(k_isai<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    k_isai<float><<<nsys, threads, smem, st>>>(p, nsys, lu, (float*)ail, (float*)aiu);
-  } else {
-    e = cudaFuncSetAttribute(k_isai<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    k_isai<double><<<nsys, threads, smem, st>>>(p, nsys, lu, (double*)ail, (double*)aiu);
-  }
-  return cudaGetLastError();
+  const int smem = (p.nnz + (p.ail_nnz > p.aiu_nnz ? p.ail_nnz : p.aiu_nnz) + (fast ? p.n : 0)) * 8;
+  void* k = fp32 ? (fast ? (void*)k_isai<float, true> : (void*)k_isai<float, false>)
+                 : (fast ? (void*)k_isai<double, true> : (void*)k_isai<double, false>);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {const_cast<DevPattern*>(&p), &nsys, &lu, &ail, &aiu};
+  return cudaLaunchKernel(k, dim3(nsys), dim3(threads), args, (size_t)smem, st);
 }
 
 cudaError_t launch_to_float(const double* a, float* b, size_t n, cudaStream_t st) {

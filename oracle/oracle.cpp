@@ -429,8 +429,11 @@ ORC_API int orc_isai_pattern(int n, const int* rp, const int* ci, int power, con
 //   general T (tri = 2): Gauss-Jordan with partial pivoting, rhs e_pos(i).
 // T is given in the reference's separate CSR form (t_rp/t_ci/t_vals; for L
 // the explicit unit diagonal is part of the pattern).
-ORC_API int orc_isai_values(int n, const int* t_rp, const int* t_ci, int t_nnz, int nsys, const double* t_vals,
-                            int tri, const int* ai_rp, const int* ai_ci, int ai_nnz, double* ai_vals) {
+// fast = 1: the library's BILU_REDUCE_FAST ISAI of an upper triangle (k_isai
+// with FAST): each division by a diagonal entry is a multiplication by its
+// correctly rounded reciprocal 1.0 / u.
+ORC_API int orc_isai_values_ex(int n, const int* t_rp, const int* t_ci, int t_nnz, int nsys, const double* t_vals,
+                               int tri, const int* ai_rp, const int* ai_ci, int ai_nnz, double* ai_vals, int fast) {
   for (int i = 0; i < n; ++i)
     if (ai_rp[i + 1] - ai_rp[i] > 32) return -1;
 #pragma omp parallel for schedule(static)
@@ -459,7 +462,7 @@ ORC_API int orc_isai_values(int n, const int* t_rp, const int* t_ci, int t_nnz, 
       } else if (tri == 1) {
         for (int t = 0; t < sz; ++t) sol[t] = (t == 0) ? 1.0 : 0.0;
         for (int col = 0; col < sz; ++col) {
-          sol[col] = sol[col] / loc[col][col];
+          sol[col] = fast ? sol[col] * (1.0 / loc[col][col]) : sol[col] / loc[col][col];
           const double top = sol[col];
           for (int t = col + 1; t < sz; ++t) sol[t] = std::fma(-top, loc[t][col], sol[t]);
         }
@@ -521,6 +524,11 @@ ORC_API int orc_isai_values(int n, const int* t_rp, const int* t_ci, int t_nnz, 
 // tol_mode: 0 = absolute (||r|| < tol, the reference's ATOL), 1 = relative to ||b||.
 // Outputs per system: x, iteration count (0.5 steps), conv flag (1/-1),
 // recursive residual norm and a detailed status (BILU_SYS_* values).
+ORC_API int orc_isai_values(int n, const int* t_rp, const int* t_ci, int t_nnz, int nsys, const double* t_vals,
+                            int tri, const int* ai_rp, const int* ai_ci, int ai_nnz, double* ai_vals) {
+  return orc_isai_values_ex(n, t_rp, t_ci, t_nnz, nsys, t_vals, tri, ai_rp, ai_ci, ai_nnz, ai_vals, 0);
+}
+
 ORC_API void orc_bicgstab(int n, int nnz, const int* rp, const int* ci, int nsys, const double* A, const double* b,
                           int f_nnz, const int* f_rp, const int* f_ci, int prec, const double* lu,
                           const float* lu_f32, int ail_nnz, const int* ail_rp,
