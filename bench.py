@@ -66,6 +66,12 @@ SECONDARY = [
 ]
 
 
+# DRAM bytes (read + write) of one register-resident solver launch on the headline workload, per
+# system: ncu dram__bytes_read.sum + dram__bytes_write.sum of a 3072-system launch (413.8 MB) / 3072;
+# the traffic grows in proportion to the systems of a launch.
+RR_TRAFFIC_BYTES_PER_SYSTEM = 134_689
+
+
 def bytes_per_system(n, nnz):
     """Compulsory HBM bytes of one solved system: A values, b, x, 24 B of results."""
     return 8 * nnz + 16 * n + 24
@@ -398,7 +404,11 @@ def main():
     ap.add_argument("--kernel-only", action="store_true",
                     help="headline solve only: no e2e pass, secondary workloads or CPU baseline (profiling runs)")
     ap.add_argument("--nsys", type=int, default=0, help="override the headline batch size (profiling runs)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the plan's default solver configuration (profiling runs: fixed launch sequence)")
     args = ap.parse_args()
+    if args.no_autotune:
+        HEADLINE["autotune"] = False
     if args.nsys > 0:
         HEADLINE["nsys"] = args.nsys
         HEADLINE["desc"] = HEADLINE["desc"].replace("4096 FP64", f"{args.nsys} FP64")
@@ -505,7 +515,8 @@ def main():
         "e2e": res["e2e"],
         "gpu_launches": 3 * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_bicgstab_rr (register-resident solver)" if info["solver_kernel"] == 1 else "k_bicgstab (solver)",
+                     "traffic": RR_TRAFFIC_BYTES_PER_SYSTEM * nsys if info["solver_kernel"] == 1 and fp32_prec
+                     else None, "traffic_source": "ncu capture of 3072 systems, scaled per system", "peak_kind": peak_kind, "kernel": "k_bicgstab_rr (register-resident solver)" if info["solver_kernel"] == 1 else "k_bicgstab (solver)",
                      "bytes_per_system": bps},
         "roofline_fp64": {"achieved": flops / solve_s / 1e9, "peak": fp64_peak, "unit": "GFLOP/s",
                           "frac": flops / solve_s / 1e9 / fp64_peak,

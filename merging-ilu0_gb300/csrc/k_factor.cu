@@ -150,32 +150,30 @@ __global__ void __launch_bounds__(512) k_parilu0(const DevPattern P, int nsys, c
         s = fma(cur[d.x], cur[d.y], s);
       }
       const int i = __ldg(P.row_of + k), j = __ldg(P.ci + k);
-      if (track) {
-        const double lu = (j < i) ? fma(cur[k], cur[__ldg(P.diag + j)], s) : s + cur[k];
-        const double r = As[k] - lu;
+      const double as = As[k] - s;
+      if (track) {  // (A - LU)_ij = (a - s) - l_ij u_jj below the diagonal, (a - s) - u_ij on or above it
+        const double r = (j < i) ? fma(-cur[k], cur[__ldg(P.diag + j)], as) : as - cur[k];
         r2 = fma(r, r, r2);
       }
-      if (!last) {
-        double v = As[k] - s;
-        if (j < i) v = FAST ? v * rinv[j] : v / cur[__ldg(P.diag + j)];
-        nxt[k] = v;
-      }
+      if (!last) nxt[k] = (j < i) ? (FAST ? as * rinv[j] : as / cur[__ldg(P.diag + j)]) : as;
     }
     // lower entries without pairs: the sum is 0, so l = a / u_jj (a - 0 == a exactly)
     const int lend = P.pl_ndep + P.pl_nlow;
     for (int q = P.pl_ndep + threadIdx.x; q < lend; q += blockDim.x) {
       const int k = __ldg(P.pl_ent + q), j = __ldg(P.ci + k);
       if (track) {
-        const double r = As[k] - fma(cur[k], cur[__ldg(P.diag + j)], 0.0);
+        const double r = fma(-cur[k], cur[__ldg(P.diag + j)], As[k]);
         r2 = fma(r, r, r2);
       }
       if (!last) nxt[k] = FAST ? As[k] * rinv[j] : As[k] / cur[__ldg(P.diag + j)];
     }
-    // upper entries without pairs: u = a, no arithmetic
+    // upper entries without pairs: u = a, no arithmetic; their residual a - u
+    // is exactly 0 once one sweep has run, so only the initial guess is checked
+    const bool check_copies = track && it == 0;
     for (int q = lend + threadIdx.x; q < nnz; q += blockDim.x) {
       const int k = __ldg(P.pl_ent + q);
-      if (track) {
-        const double r = As[k] - (0.0 + cur[k]);
+      if (check_copies) {
+        const double r = As[k] - cur[k];
         r2 = fma(r, r, r2);
       }
       if (!last) nxt[k] = As[k];

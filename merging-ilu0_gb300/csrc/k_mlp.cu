@@ -330,17 +330,29 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// Warm start of one system per CTA.  Entries with no dependency pairs on or
-// above the diagonal converge to a_ij exactly and are copied.  The others go
-// through the network in tiles of 16 per warp: lanes 0-15 form one entry's
-// features; every lane then forms the first-layer activations it needs for
-// the A fragments of the m16n8k16 MMAs (rows g and g+8, k = 2t, 2t+1, 2t+8,
-// 2t+9 of each 16-wide chunk; g = lane/4, t = lane%4), split into BF16 high
-// and low parts; layer 2 is 2 x 4 x 8 MMAs against W2 (BF16, B fragments
-// straight from shared memory); GELU and the output layer reduce over the 4
-// lanes of a quad.  The ILU residual ||(A - L0 U0)|_S||_F / ||A||_F then
-// decides between the prediction and the plain initialisation lu0 = A.
+// Warm start: persistent CTAs over the systems (the network's weights are
+// staged once per CTA).  Entries with no dependency pairs on or above the
+// diagonal converge to a_ij exactly and are copied.  The others go through the
+// network in tiles of 32 per warp: every lane forms one entry's features, then
+// each 16-entry half runs as m16n8k16 MMAs -- every lane forms the first-layer
+// activations it needs for its A fragments (rows g and g+8, k = 2t, 2t+1,
+// 2t+8, 2t+9 of each 16-wide chunk; g = lane/4, t = lane%4), split into BF16
+// high and low parts; layer 2 is 2 x 4 x 8 MMAs against W2 (BF16); GELU and
+// the output layer reduce over the 4 lanes of a quad.  The ILU residual
+// ||(A - L0 U0)|_S||_F / ||A||_F then decides between the prediction and the
+// plain initialisation lu0 = A.
+//
+// Shared-memory weight layout, arranged so that each lane fetches its operands
+// with 128-bit loads (the kernel is bound by shared-memory traffic otherwise):
+//   w1p [64][12]     hidden unit v: W1[v][0..8], b1[v], 0, 0
+//   bw  [8][4] x 4   slice ut, quad index t: b2[u], b2[u+1], w3[u], w3[u+1], u = 8 ut + 2 t
+//   b3  [4]          b3, 0, 0, 0
+//   w2f [8][32][8]   slice ut, lane: its B fragments of the 4 k-chunks, (W2 row 8 ut + g,
+//                    words 8 ch + t and 8 ch + 4 + t) for ch = 0..3
 constexpr int WARM_THREADS = 256;
+constexpr int WP_W1 = 0, WP_BW = H * 12, WP_B3 = WP_BW + 8 * 4 * 4, WP_W2 = WP_B3 + 4;
+constexpr int WP_WORDS = WP_W2 + 8 * 32 * 8;
+static_assert(WP_W2 % 4 == 0 && WP_WORDS % 4 == 0, "16-byte aligned weight blocks");
 
 __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, int nsys,
                                                            const double* __restrict__ A,
@@ -351,157 +363,170 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
                                                            double* __restrict__ LU0, double* __restrict__ res_out,
                                                            int* __restrict__ used) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  float* w1 = reinterpret_cast<float*>(smraw);     // W1 [64][9] then b1 [64]
-  float* b1 = w1 + H * NF;
-  float* b2 = b1 + H;
-  float* w3 = b2 + H;
-  float* b3 = w3 + H;                               // 1 (padded to 4)
-  __nv_bfloat16* w2 = reinterpret_cast<__nv_bfloat16*>(b3 + 4);  // [64][64]
-  double* lu = reinterpret_cast<double*>(w2 + H * H);
+  float* wp = reinterpret_cast<float*>(smraw);
+  uint32_t* w2f = reinterpret_cast<uint32_t*>(wp + WP_W2);
+  double* lu = reinterpret_cast<double*>(wp + WP_WORDS);
   __shared__ double s_num[WARM_THREADS / 32], s_den[WARM_THREADS / 32];
   __shared__ int s_ok;
-  const int s = blockIdx.x;
-  if (s >= nsys) return;
-  for (int k = threadIdx.x; k < H * NF; k += blockDim.x) w1[k] = __bfloat162float(pbf[OW1 + k]);
-  for (int k = threadIdx.x; k < H; k += blockDim.x) {
-    b1[k] = __bfloat162float(pbf[OB1 + k]);
-    b2[k] = __bfloat162float(pbf[OB2 + k]);
-    w3[k] = __bfloat162float(pbf[OW3 + k]);
+  for (int k = threadIdx.x; k < H * 12; k += blockDim.x) {
+    const int v = k / 12, c = k % 12;
+    wp[WP_W1 + k] = c < NF ? __bfloat162float(pbf[OW1 + v * NF + c]) : (c == NF ? __bfloat162float(pbf[OB1 + v]) : 0.0f);
   }
-  if (threadIdx.x == 0) b3[0] = __bfloat162float(pbf[OB3]);
-  for (int k = threadIdx.x; k < H * H; k += blockDim.x) w2[k] = pbf[OW2 + k];
-  const double* As = A + (size_t)s * P.nnz;
-  for (int e = threadIdx.x; e < P.nnz; e += blockDim.x) lu[e] = As[e];  // exact for the copied entries
-  __syncthreads();
+  for (int k = threadIdx.x; k < 8 * 4 * 4; k += blockDim.x) {
+    const int ut = k >> 4, t = (k >> 2) & 3, c = k & 3, u = ut * 8 + 2 * t + (c & 1);
+    wp[WP_BW + k] = __bfloat162float(pbf[(c < 2 ? OB2 : OW3) + u]);
+  }
+  if (threadIdx.x < 4) wp[WP_B3 + threadIdx.x] = threadIdx.x == 0 ? __bfloat162float(pbf[OB3]) : 0.0f;
+  const uint32_t* w2g = reinterpret_cast<const uint32_t*>(pbf + OW2);  // row u: 32 words of 2 BF16
+  for (int k = threadIdx.x; k < 8 * 32 * 8; k += blockDim.x) {
+    const int ut = k >> 8, ln = (k >> 3) & 31, c = k & 7, ch = c >> 1;
+    const int g = ln >> 2, t = ln & 3;
+    w2f[k] = w2g[(ut * 8 + g) * (H / 2) + ch * 8 + (c & 1) * 4 + t];
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const int g = lane >> 2, t = lane & 3;
-  const int ntile = (P.n_mlp + 15) >> 4;
-  for (int tile = warp; tile < ntile; tile += nwarp) {
-    // features of entry tile*16 + lane (lanes 0-15)
-    const int q = tile * 16 + (lane & 15);
-    const bool live = lane < 16 && q < P.n_mlp;
-    float f[NF];
-    double ab = 0.0;
-    int e = -1;
-    if (live) {
-      e = P.mlp_ent[q];
-      const Feat ft = features(P, s, e, A, rown, coln, corr);
+  const float4* w1v = reinterpret_cast<const float4*>(wp + WP_W1);
+  const float4* bwv = reinterpret_cast<const float4*>(wp + WP_BW);
+  const uint4* w2v = reinterpret_cast<const uint4*>(w2f);
+  const float b3 = wp[WP_B3];
+  const int ntile = (P.n_mlp + 31) >> 5;
+  for (int s = blockIdx.x; s < nsys; s += gridDim.x) {
+    __syncthreads();  // weights staged / the previous system's lu and s_ok no longer read
+    const double* As = A + (size_t)s * P.nnz;
+    for (int e = threadIdx.x; e < P.nnz; e += blockDim.x) lu[e] = As[e];  // exact for the copied entries
+    __syncthreads();
+    for (int tile = warp; tile < ntile; tile += nwarp) {
+      // features of entry tile*32 + lane
+      const int q = tile * 32 + lane;
+      const bool live = q < P.n_mlp;
+      float f[NF];
+      double ab = 0.0;
+      int e = -1;
+      if (live) {
+        e = P.mlp_ent[q];
+        const Feat ft = features(P, s, e, A, rown, coln, corr);
 #pragma unroll
-      for (int k = 0; k < NF; ++k) f[k] = ft.f[k];
-      ab = ft.a * (double)ft.base;
-    } else {
+        for (int k = 0; k < NF; ++k) f[k] = ft.f[k];
+        ab = ft.a * (double)ft.base;
+      } else {
 #pragma unroll
-      for (int k = 0; k < NF; ++k) f[k] = 0.0f;
-    }
-    float xa[NF], xb[NF];  // rows g and g+8
+        for (int k = 0; k < NF; ++k) f[k] = 0.0f;
+      }
+#pragma unroll 1
+      for (int half = 0; half < 2; ++half) {
+        float xa[NF], xb[NF];  // rows g and g+8 of this half
 #pragma unroll
-    for (int k = 0; k < NF; ++k) {
-      xa[k] = __shfl_sync(kFull, f[k], g);
-      xb[k] = __shfl_sync(kFull, f[k], g + 8);
-    }
-    // first layer on CUDA cores, straight into A fragments (high and low parts)
-    uint32_t ahi[4][4], alo[4][4];
-#pragma unroll
-    for (int ch = 0; ch < 4; ++ch) {
-#pragma unroll
-      for (int half = 0; half < 2; ++half) {  // k = 2t, 2t+1 (half 0) and 2t+8, 2t+9 (half 1)
-        const int v0 = ch * 16 + 2 * t + 8 * half;
-        float ha[2], hb[2];
-#pragma unroll
-        for (int d = 0; d < 2; ++d) {
-          const int v = v0 + d;
-          float pa = b1[v], pb = b1[v];
-#pragma unroll
-          for (int k = 0; k < NF; ++k) {
-            pa = fmaf(w1[v * NF + k], xa[k], pa);
-            pb = fmaf(w1[v * NF + k], xb[k], pb);
-          }
-          ha[d] = gelu_fast(pa);
-          hb[d] = gelu_fast(pb);
+        for (int k = 0; k < NF; ++k) {
+          xa[k] = __shfl_sync(kFull, f[k], 16 * half + g);
+          xb[k] = __shfl_sync(kFull, f[k], 16 * half + g + 8);
         }
-        const float ha0h = __bfloat162float(__float2bfloat16_rn(ha[0]));
-        const float ha1h = __bfloat162float(__float2bfloat16_rn(ha[1]));
-        const float hb0h = __bfloat162float(__float2bfloat16_rn(hb[0]));
-        const float hb1h = __bfloat162float(__float2bfloat16_rn(hb[1]));
-        ahi[ch][2 * half + 0] = pack_bf16(ha0h, ha1h);
-        ahi[ch][2 * half + 1] = pack_bf16(hb0h, hb1h);
-        alo[ch][2 * half + 0] = pack_bf16(ha[0] - ha0h, ha[1] - ha1h);
-        alo[ch][2 * half + 1] = pack_bf16(hb[0] - hb0h, hb[1] - hb1h);
+        // first layer on CUDA cores, straight into A fragments (high and low parts)
+        uint32_t ahi[4][4], alo[4][4];
+#pragma unroll
+        for (int ch = 0; ch < 4; ++ch) {
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {  // k = 2t, 2t+1 (hh 0) and 2t+8, 2t+9 (hh 1)
+            const int v0 = ch * 16 + 2 * t + 8 * hh;
+            float ha[2], hb[2];
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+              const float4 wa = w1v[(v0 + d) * 3], wb = w1v[(v0 + d) * 3 + 1], wc = w1v[(v0 + d) * 3 + 2];
+              const float w[NF] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w, wc.x};
+              float pa = wc.y, pb = wc.y;  // b1
+#pragma unroll
+              for (int k = 0; k < NF; ++k) {
+                pa = fmaf(w[k], xa[k], pa);
+                pb = fmaf(w[k], xb[k], pb);
+              }
+              ha[d] = gelu_fast(pa);
+              hb[d] = gelu_fast(pb);
+            }
+            const float ha0h = __bfloat162float(__float2bfloat16_rn(ha[0]));
+            const float ha1h = __bfloat162float(__float2bfloat16_rn(ha[1]));
+            const float hb0h = __bfloat162float(__float2bfloat16_rn(hb[0]));
+            const float hb1h = __bfloat162float(__float2bfloat16_rn(hb[1]));
+            ahi[ch][2 * hh + 0] = pack_bf16(ha0h, ha1h);
+            ahi[ch][2 * hh + 1] = pack_bf16(hb0h, hb1h);
+            alo[ch][2 * hh + 0] = pack_bf16(ha[0] - ha0h, ha[1] - ha1h);
+            alo[ch][2 * hh + 1] = pack_bf16(hb[0] - hb0h, hb[1] - hb1h);
+          }
+        }
+        // register order of the A fragment: a0 (row g, k 2t..), a1 (row g+8, k 2t..), a2 (row g, k 2t+8..),
+        // a3 (row g+8, k 2t+8..)
+        float outa = 0.0f, outb = 0.0f;
+#pragma unroll
+        for (int ut = 0; ut < 8; ++ut) {
+          float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+          const uint4 q0 = w2v[(ut * 32 + lane) * 2], q1 = w2v[(ut * 32 + lane) * 2 + 1];
+          const uint32_t bfr[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+#pragma unroll
+          for (int ch = 0; ch < 4; ++ch) {
+            const uint32_t ah[4] = {ahi[ch][0], ahi[ch][1], ahi[ch][2], ahi[ch][3]};
+            const uint32_t al[4] = {alo[ch][0], alo[ch][1], alo[ch][2], alo[ch][3]};
+            mma_bf16(c, ah, bfr[2 * ch], bfr[2 * ch + 1]);
+            mma_bf16(c, al, bfr[2 * ch], bfr[2 * ch + 1]);
+          }
+          const float4 bw = bwv[ut * 4 + t];  // b2[u], b2[u+1], w3[u], w3[u+1]
+          outa = fmaf(bw.z, gelu_fast(c[0] + bw.x), outa);
+          outa = fmaf(bw.w, gelu_fast(c[1] + bw.y), outa);
+          outb = fmaf(bw.z, gelu_fast(c[2] + bw.x), outb);
+          outb = fmaf(bw.w, gelu_fast(c[3] + bw.y), outb);
+        }
+        outa += __shfl_xor_sync(kFull, outa, 1);
+        outa += __shfl_xor_sync(kFull, outa, 2);
+        outb += __shfl_xor_sync(kFull, outb, 1);
+        outb += __shfl_xor_sync(kFull, outb, 2);
+        // the entry of row r (0..15) of this half lives on lane 16*half + r; rows r < 8
+        // were reduced on lane 4r (outa), rows 8..15 on lane 4(r-8) (outb)
+        const int r = lane & 15;
+        const float ya = __shfl_sync(kFull, outa, (r & 7) << 2);
+        const float yb = __shfl_sync(kFull, outb, (r & 7) << 2);
+        if (live && (lane >> 4) == half) {
+          const float y = (r < 8 ? ya : yb) + b3;
+          lu[e] = ab * (1.0 + (double)y);
+        }
       }
     }
-    // register order of the A fragment: a0 (row g, k 2t..), a1 (row g+8, k 2t..), a2 (row g, k 2t+8..),
-    // a3 (row g+8, k 2t+8..)
-    float outa = 0.0f, outb = 0.0f;
-#pragma unroll
-    for (int ut = 0; ut < 8; ++ut) {
-      float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      const uint32_t* wrow = reinterpret_cast<const uint32_t*>(w2 + (ut * 8 + g) * H);
-#pragma unroll
-      for (int ch = 0; ch < 4; ++ch) {
-        const uint32_t bb0 = wrow[ch * 8 + t];      // W2[u][16ch + 2t], [.. + 1]
-        const uint32_t bb1 = wrow[ch * 8 + 4 + t];  // W2[u][16ch + 2t + 8], [.. + 9]
-        const uint32_t ah[4] = {ahi[ch][0], ahi[ch][1], ahi[ch][2], ahi[ch][3]};
-        const uint32_t al[4] = {alo[ch][0], alo[ch][1], alo[ch][2], alo[ch][3]};
-        mma_bf16(c, ah, bb0, bb1);
-        mma_bf16(c, al, bb0, bb1);
+    __syncthreads();
+    // residual of the warm start: (A - LU)_ij = a_ij - sum_{k<min(i,j)} l_ik u_kj - (l_ij u_jj | u_ij)
+    double num = 0.0, den = 0.0;
+    for (int e = threadIdx.x; e < P.nnz; e += blockDim.x) {
+      const int i = P.row_of[e], j = P.ci[e];
+      double acc = 0.0;
+      for (int q = P.dep_ptr[e]; q < P.dep_ptr[e + 1]; ++q) {
+        const int2 d = P.dep[q];
+        acc = fma(lu[d.x], lu[d.y], acc);
       }
-      const int u = ut * 8 + 2 * t;
-      outa = fmaf(w3[u], gelu_fast(c[0] + b2[u]), outa);
-      outa = fmaf(w3[u + 1], gelu_fast(c[1] + b2[u + 1]), outa);
-      outb = fmaf(w3[u], gelu_fast(c[2] + b2[u]), outb);
-      outb = fmaf(w3[u + 1], gelu_fast(c[3] + b2[u + 1]), outb);
+      acc = (j < i) ? fma(lu[e], lu[P.diag[j]], acc) : acc + lu[e];
+      const double rr = As[e] - acc;
+      num = fma(rr, rr, num);
+      den = fma(As[e], As[e], den);
     }
-    outa += __shfl_xor_sync(kFull, outa, 1);
-    outa += __shfl_xor_sync(kFull, outa, 2);
-    outb += __shfl_xor_sync(kFull, outb, 1);
-    outb += __shfl_xor_sync(kFull, outb, 2);
-    // entry of row g lives on lane g, of row g+8 on lane g+8
-    const float yg = __shfl_sync(kFull, outa, (lane & 7) << 2);        // lane r (< 8) gets row r
-    const float yg8 = __shfl_sync(kFull, outb, ((lane - 8) & 7) << 2);  // lane r (8..15) gets row r
-    if (live) {
-      const float y = (lane < 8 ? yg : yg8) + b3[0];
-      lu[e] = ab * (1.0 + (double)y);
-    }
-  }
-  __syncthreads();
-  // residual of the warm start: (A - LU)_ij = a_ij - sum_{k<min(i,j)} l_ik u_kj - (l_ij u_jj | u_ij)
-  double num = 0.0, den = 0.0;
-  for (int e = threadIdx.x; e < P.nnz; e += blockDim.x) {
-    const int i = P.row_of[e], j = P.ci[e];
-    double acc = 0.0;
-    for (int q = P.dep_ptr[e]; q < P.dep_ptr[e + 1]; ++q) {
-      const int2 d = P.dep[q];
-      acc = fma(lu[d.x], lu[d.y], acc);
-    }
-    acc = (j < i) ? fma(lu[e], lu[P.diag[j]], acc) : acc + lu[e];
-    const double r = As[e] - acc;
-    num = fma(r, r, num);
-    den = fma(As[e], As[e], den);
-  }
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    num += __shfl_down_sync(kFull, num, off);
-    den += __shfl_down_sync(kFull, den, off);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    s_num[threadIdx.x >> 5] = num;
-    s_den[threadIdx.x >> 5] = den;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a = 0.0, b = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      a += s_num[w];
-      b += s_den[w];
+    for (int off = 16; off > 0; off >>= 1) {
+      num += __shfl_down_sync(kFull, num, off);
+      den += __shfl_down_sync(kFull, den, off);
     }
-    const double res = b > 0.0 ? sqrt(a / b) : sqrt(a);
-    s_ok = (res <= threshold) ? 1 : 0;  // NaN fails the test: fallback
-    if (res_out) res_out[s] = res;
-    if (used) used[s] = s_ok;
+    if (lane == 0) {
+      s_num[warp] = num;
+      s_den[warp] = den;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0.0, b = 0.0;
+      for (int w = 0; w < nwarp; ++w) {
+        a += s_num[w];
+        b += s_den[w];
+      }
+      const double res = b > 0.0 ? sqrt(a / b) : sqrt(a);
+      s_ok = (res <= threshold) ? 1 : 0;  // NaN fails the test: fallback
+      if (res_out) res_out[s] = res;
+      if (used) used[s] = s_ok;
+    }
+    __syncthreads();
+    const int ok = s_ok;
+    for (int e = threadIdx.x; e < P.nnz; e += blockDim.x) LU0[(size_t)s * P.nnz + e] = ok ? lu[e] : As[e];
   }
-  __syncthreads();
-  const int ok = s_ok;
-  for (int e = threadIdx.x; e < P.nnz; e += blockDim.x) LU0[(size_t)s * P.nnz + e] = ok ? lu[e] : As[e];
 }
 
 }  // namespace
@@ -557,10 +582,16 @@ cudaError_t launch_mlp_warm(const DevPattern& p, int nsys, const double* A, cons
                             const float* corr, const void* pbf, double threshold, double* lu0, double* res, int* used,
                             cudaStream_t st) {
   if (nsys == 0) return cudaSuccess;
-  const size_t smem = sizeof(float) * (H * NF + 3 * H + 4) + 2 * H * H + sizeof(double) * p.nnz;
+  const size_t smem = sizeof(float) * WP_WORDS + sizeof(double) * p.nnz;
   cudaError_t e = cudaFuncSetAttribute(k_mlp_warm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_mlp_warm<<<nsys, WARM_THREADS, smem, st>>>(p, nsys, A, rown, coln, corr, (const __nv_bfloat16*)pbf, threshold,
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mlp_warm, WARM_THREADS, smem);
+  if (e != cudaSuccess) return e;
+  const int grid = nsys < nsm * (occ > 0 ? occ : 1) ? nsys : nsm * (occ > 0 ? occ : 1);
+  k_mlp_warm<<<grid, WARM_THREADS, smem, st>>>(p, nsys, A, rown, coln, corr, (const __nv_bfloat16*)pbf, threshold,
                                                lu0, res, used);
   return cudaGetLastError();
 }
