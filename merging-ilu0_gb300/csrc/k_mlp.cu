@@ -56,23 +56,25 @@ __global__ void k_rowstats(const DevPattern P, int nsys, const double* __restric
                            float* __restrict__ coln, float* __restrict__ corr) {
   const int s = blockIdx.x;
   if (s >= nsys) return;
+  // FP32 throughout (the features are FP32): FP64 division and square root
+  // are long instruction sequences on this part's FP64 pipe
   const double* As = A + (size_t)s * P.nnz;
   for (int i = threadIdx.x; i < P.n; i += blockDim.x) {
     const int b = P.rp[i], e = P.rp[i + 1], d = P.diag[i];
-    double rn = 0.0, cn = 0.0, c = 0.0;
+    float rn = 0.0f, cn = 0.0f, c = 0.0f;
     for (int k = b; k < e; ++k) {
-      const double a = As[k];
-      rn = fma(a, a, rn);
+      const float a = (float)As[k];
+      rn = fmaf(a, a, rn);
       const int t = P.tpos[k];
       if (t >= 0) {
-        const double at = As[t];
-        cn = fma(at, at, cn);
-        if (k < d) c = fma(a, at / As[P.diag[P.ci[k]]], c);
+        const float at = (float)As[t];
+        cn = fmaf(at, at, cn);
+        if (k < d) c = fmaf(a, at / (float)As[P.diag[P.ci[k]]], c);
       }
     }
-    rown[(size_t)s * P.n + i] = (float)sqrt(rn);
-    coln[(size_t)s * P.n + i] = (float)sqrt(cn);
-    corr[(size_t)s * P.n + i] = (float)c;
+    rown[(size_t)s * P.n + i] = sqrtf(rn);
+    coln[(size_t)s * P.n + i] = sqrtf(cn);
+    corr[(size_t)s * P.n + i] = c;
   }
 }
 
@@ -383,6 +385,7 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
     const int g = ln >> 2, t = ln & 3;
     w2f[k] = w2g[(ut * 8 + g) * (H / 2) + ch * 8 + (c & 1) * 4 + t];
   }
+  __syncthreads();  // staged weights visible to every warp before b3 is read below
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const int g = lane >> 2, t = lane & 3;
   const float4* w1v = reinterpret_cast<const float4*>(wp + WP_W1);
@@ -391,7 +394,7 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
   const float b3 = wp[WP_B3];
   const int ntile = (P.n_mlp + 31) >> 5;
   for (int s = blockIdx.x; s < nsys; s += gridDim.x) {
-    __syncthreads();  // weights staged / the previous system's lu and s_ok no longer read
+    __syncthreads();  // the previous system's lu and s_ok no longer read
     const double* As = A + (size_t)s * P.nnz;
     for (int e = threadIdx.x; e < P.nnz; e += blockDim.x) lu[e] = As[e];  // exact for the copied entries
     __syncthreads();

@@ -957,19 +957,21 @@ ORC_API void orc_mlp_features(int n, int nnz, const int* rp, const int* ci, int 
     const long long g = idx[q];
     const int s = (int)(g / nnz), e = (int)(g % nnz);
     const double* As = vals + (size_t)s * nnz;
-    auto stats = [&](int r, float& rn, float& cn, float& cr) {
-      double a = 0.0, b = 0.0, c = 0.0;
+    auto stats = [&](int r, float& rn, float& cn, float& cr) {  // FP32, as k_rowstats
+      float a = 0.0f, b = 0.0f, c = 0.0f;
       for (int k = rp[r]; k < rp[r + 1]; ++k) {
-        a = std::fma(As[k], As[k], a);
+        const float ak = (float)As[k];
+        a = std::fma(ak, ak, a);
         const int t = tpos[k];
         if (t >= 0) {
-          b = std::fma(As[t], As[t], b);
-          if (k < diag[r]) c = std::fma(As[k], As[t] / As[diag[ci[k]]], c);
+          const float at = (float)As[t];
+          b = std::fma(at, at, b);
+          if (k < diag[r]) c = std::fma(ak, at / (float)As[diag[ci[k]]], c);
         }
       }
-      rn = (float)std::sqrt(a);
-      cn = (float)std::sqrt(b);
-      cr = (float)c;
+      rn = std::sqrt(a);
+      cn = std::sqrt(b);
+      cr = c;
     };
     const int i = rowof[e], j = ci[e];
     float rni, cni, cri, rnj, cnj, crj;

@@ -63,9 +63,12 @@ def test_tensor_core_inference_matches_oracle(cuda):
         m.train(plan, V, LU, 50, 2048, 3e-3, seed=2)
         LU0 = torch.empty_like(V)
         m.warm_start(plan, V, LU0, 1e30)  # accept everything
+        LU1 = torch.full_like(V, float("nan"))
+        m.warm_start(plan, V, LU1, 1e30)  # a second call gives the same bits
         torch.cuda.synchronize()
         params = m.params()
     got = LU0.cpu().numpy()
+    H.assert_bitwise(LU1.cpu().numpy(), got, "repeated warm start")
     d = O.find_diag(rp, ci)
     n = len(rp) - 1
     deps = O.parilu0(rp, ci, v[:1], 0)  # shape only
