@@ -171,10 +171,11 @@ __host__ __device__ inline SmemLayout layout_for(int n, int annz, int fnnz, int 
 
 // Shared-memory carve-up of the register-resident FAST solver (k_solve_rr.cu):
 // reduction slots, the SpMV input (FP64), the preconditioner input and
-// intermediate (FT), then optionally A and the ISAI values.  -1 = not used /
-// read from global memory.
+// intermediate (FT), for LU preconditioners the in-place factors (FP64 while
+// the kernel factorises, FT after) and the diagonal reciprocals, then
+// optionally A and the ISAI values.  -1 = not used / read from global memory.
 struct RRLayout {
-  int red = -1, ph = -1, in = -1, mid = -1, A = -1, ail = -1, aiu = -1, total = 0;
+  int red = -1, ph = -1, in = -1, mid = -1, F = -1, rinv = -1, A = -1, ail = -1, aiu = -1, total = 0;
 };
 
 // One system of an uneven batch (own size and pattern); offsets in ints into

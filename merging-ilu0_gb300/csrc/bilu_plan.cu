@@ -273,20 +273,22 @@ void choose_layout(bilu_plan& P) {
   P.threads = th;
 }
 
-// Register-resident FAST solver: FAST order, ISAI or no preconditioner, at most
+// Register-resident FAST solver: FAST order, any preconditioner kind, at most
 // 8 rows per thread.  rr_configure sets the plan up for `nt` threads per system
 // and the shared-memory staging `mask` (bit 0 A, bit 1 aiL / aiA, bit 2 aiU;
 // operands that would cost occupancy are left in global memory, read through
-// L1); false when the kernel does not apply or that configuration is invalid.
+// L1; ILU factors are always staged); false when the kernel does not apply or
+// that configuration is invalid.
 bool rr_configure(bilu_plan& P, int nt, int mask) {
   const bilu_options& o = P.opts;
   const int pk = prec_kind(o.precond);
-  if (o.reduction != BILU_REDUCE_FAST || (pk != PK_ISAI && pk != PK_NONE)) return false;
+  if (o.reduction != BILU_REDUCE_FAST) return false;
   const int n = P.n;
   nt = std::max(round_up(nt, 32), 32);
   const int R = rr_rows_per_thread(n, nt);
   if (R == 0 || nt > rr_max_threads(R)) return false;
-  const int pv = pk == PK_NONE ? 0 : (P.general_isai ? 2 : 1);
+  const bool lu = (pk == PK_ILU_INKERNEL || pk == PK_LU_GLOBAL);
+  const int pv = pk == PK_NONE ? 0 : (lu ? 3 : (P.general_isai ? 2 : 1));
   const bool fp32 = is_fp32(o);
   const int fts = fp32 ? 4 : 8;
   RRLayout L;
@@ -297,8 +299,13 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   };
   take(L.red, 4 * 64 * 8);
   take(L.ph, (long long)n * 8);
-  if (pv != 0) take(L.in, (long long)n * fts);
+  if (pv == 1 || pv == 2 || (pv == 3 && fp32)) take(L.in, (long long)n * fts);
   if (pv == 1) take(L.mid, (long long)n * fts);
+  if (pv == 3) {
+    // the merged form factorises in FP64 in this slot before rounding to FT
+    take(L.F, (long long)P.nnz * (pk == PK_ILU_INKERNEL ? 8 : fts));
+    take(L.rinv, (long long)n * fts);
+  }
   int dev = 0, per_sm = 0, reserved = 0, optin = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
@@ -316,7 +323,7 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
     if ((mask & bit) && bytes > 0 && off + bytes <= budget) take(dst, bytes);
   };
   stage(L.A, (long long)P.nnz_in * 8, 1);
-  if (pv != 0) stage(L.ail, (long long)P.ail_rp[n] * fts, 2);
+  if (pv == 1 || pv == 2) stage(L.ail, (long long)P.ail_rp[n] * fts, 2);
   if (pv == 1) stage(L.aiu, (long long)P.aiu_rp[n] * fts, 4);
   L.total = off;
   P.rr = true;

@@ -1,11 +1,13 @@
 // Register-resident batched BiCGSTAB for BILU_REDUCE_FAST with an ISAI
-// preconditioner (two triangles or the general ISAI of A) or none.
+// preconditioner (two triangles or the general ISAI of A), in-place ILU
+// factors (factorised in the kernel, the merged form, or given) or none.
 //
 // Same method, exits and iteration counting as the shared-memory kernel
-// (k_solve.cu, after PrecondBiCGSTAB_ilu_isai_gpu.cu:89-257 and
-// Bicgstab_common.hpp:195-250); only the reduction order differs, and it is
-// fixed by (threads per system, rows per thread), so the oracle restates it
-// bit for bit (orc_bicgstab_fast).
+// (k_solve.cu, after PrecondBiCGSTAB_exact_ilu0_app1_merged_gpu.cu:249-538,
+// PrecondBiCGSTAB_ilu_isai_gpu.cu:89-257 and Bicgstab_common.hpp:195-250);
+// only the reduction order differs, and it is fixed by (threads per system,
+// rows per thread), so the oracle restates it bit for bit
+// (orc_bicgstab_fast).
 //
 // GB300 mapping.  FP64 issue is the bound (about two FP64 lane-operations per
 // clock per SM, one warp instruction costs the same whatever its active
@@ -26,7 +28,11 @@
 //   * the CTA is small (one warp for n <= 256), so several systems share an SM
 //     and one system's barrier or reduction latency overlaps another's FMAs;
 //   * with FP32 ISAI values (BILU_FP32) both preconditioner SpMVs run on the
-//     FP32 pipe; FP64 stays in A*x, the inner products and the recurrences.
+//     FP32 pipe; FP64 stays in A*x, the inner products and the recurrences;
+//   * ILU factors live in shared memory (the merged form factorises there,
+//     rows in level order as the shared-memory kernel does); the triangular
+//     solves run level by level over the whole CTA, in place on the
+//     preconditioner vector, one barrier per level.
 //
 // Reduction order (what orc_bicgstab_fast restates):
 //   thread partial   d = fma(a_i, b_i, d) over its rows in k order, from 0.0
@@ -34,6 +40,11 @@
 //   block            s = 0.0; s = s + w_j for warps j = 0 .. NT/32-1
 //   SpMV row         acc = fma(a_k, x_ci(k), acc), k ascending, from 0.0 (FP64)
 //   ISAI row (FT)    the same in FT; input rounded to FT, output widened to FP64
+//   LU solve (FT)    input rounded to FT; lower row i: s = fma(l_ik, y_k, s) over
+//                    k ascending from 0, y_i = y_i - s; upper row i: s = fma(u_ik,
+//                    z_k, s) over k descending from 0, z_i = (y_i - s) * rinv_i
+//                    with rinv_i = 1.0 / u_ii in FP64 (rounded to float for FP32
+//                    factors); z widened to FP64
 #include <cuda_runtime.h>
 
 #include "bilu_internal.h"
@@ -42,6 +53,8 @@ namespace bilu {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+
+#include "k_ilu_rows.cuh"
 
 // K values summed over the CTA; every thread returns the same sums.
 // red: K * 32 doubles of this reduction's own slot.
@@ -95,8 +108,46 @@ __device__ __forceinline__ void rows_acc(const VT* __restrict__ val, const int* 
   }
 }
 
-// PV: 0 none, 1 ISAI of L and U (z = aiU (aiL v)), 2 general ISAI (z = aiA v).
-// FT: type of the ISAI values and of the preconditioner arithmetic.
+// z = U^{-1} L^{-1} y over the CTA, level by level, in place on y (the
+// preconditioner input, already rounded to FT).  For FP32 factors the upper
+// solve also widens each z_i into zd (the FP64 SpMV input); for FP64 factors y
+// is that vector.  Ends with a barrier: z is visible to every thread.
+template <typename FT>
+__device__ __forceinline__ void lu_apply(const DevPattern& P, const FT* __restrict__ F, const FT* __restrict__ rinv,
+                                         FT* y, double* zd, int tid, int nt) {
+  const int* __restrict__ rp = P.rp;
+  const int* __restrict__ ci = P.ci;
+  const int* __restrict__ dg = P.diag;
+  for (int lev = 0; lev < P.nlev_lo; ++lev) {
+    const int b = __ldg(P.lev_lo_ptr + lev), e = __ldg(P.lev_lo_ptr + lev + 1);
+    for (int q = b + tid; q < e; q += nt) {
+      const int i = __ldg(P.lev_lo_rows + q);
+      const int beg = __ldg(rp + i), d = __ldg(dg + i);
+      FT s = FT(0);
+      for (int k = beg; k < d; ++k) s = fma_t(F[k], y[__ldg(ci + k)], s);
+      y[i] = y[i] - s;
+    }
+    __syncthreads();
+  }
+  for (int lev = 0; lev < P.nlev_up; ++lev) {
+    const int b = __ldg(P.lev_up_ptr + lev), e = __ldg(P.lev_up_ptr + lev + 1);
+    for (int q = b + tid; q < e; q += nt) {
+      const int i = __ldg(P.lev_up_rows + q);
+      const int end = __ldg(rp + i + 1), d = __ldg(dg + i);
+      FT s = FT(0);
+      for (int k = end - 1; k > d; --k) s = fma_t(F[k], y[__ldg(ci + k)], s);
+      const FT z = (y[i] - s) * rinv[i];
+      y[i] = z;
+      if (sizeof(FT) == 4) zd[i] = (double)z;
+    }
+    __syncthreads();
+  }
+}
+
+// PV: 0 none, 1 ISAI of L and U (z = aiU (aiL v)), 2 general ISAI (z = aiA v),
+// 3 in-place ILU factors (a.prec: PK_ILU_INKERNEL factorises A here,
+// PK_LU_GLOBAL reads a.F).
+// FT: type of the ISAI values / factors and of the preconditioner arithmetic.
 template <int R, int PV, typename FT>
 __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 : 128)), R == 8 ? 3 : 1)
     k_bicgstab_rr(const SolveArgs a, const RRLayout L) {
@@ -144,6 +195,51 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
     }
   }
 
+  FT* Fs = nullptr;
+  FT* rinv = nullptr;
+  if (PV == 3) {
+    Fs = reinterpret_cast<FT*>(smem + L.F);
+    rinv = reinterpret_cast<FT*>(smem + L.rinv);
+    const int nnz = P.nnz;
+    if (a.prec == PK_ILU_INKERNEL) {
+      // merged form: ILU(0) of A in FP64 in the factor slot (the factor
+      // pattern is the operator pattern: no inserted diagonals)
+      double* LUd = reinterpret_cast<double*>(smem + L.F);
+      for (int k = tid; k < nnz; k += nt) LUd[k] = __ldg(Ag + k);
+      __syncthreads();
+      ilu_rows(P, LUd, a.approach);
+      if (sizeof(FT) == 4) {
+        // round to float in place, in chunks of 8 values per thread: chunk c's
+        // float writes end at byte 4 * (its last index + 1), before the first
+        // double of any later chunk, and its own reads finish at the barrier
+        constexpr int C = 8;
+        for (int base = 0; base < nnz; base += C * nt) {
+          double tv[C];
+#pragma unroll
+          for (int c = 0; c < C; ++c) {
+            const int k = base + c * nt + tid;
+            tv[c] = k < nnz ? LUd[k] : 0.0;
+          }
+          __syncthreads();
+#pragma unroll
+          for (int c = 0; c < C; ++c) {
+            const int k = base + c * nt + tid;
+            if (k < nnz) Fs[k] = (FT)tv[c];
+          }
+        }
+      }
+    } else {
+      const FT* g = reinterpret_cast<const FT*>(a.F) + (size_t)sys * nnz;
+      for (int k = tid; k < nnz; k += nt) Fs[k] = g[k];
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) {
+      const double dgi = (double)Fs[__ldg(P.diag + i)];
+      rinv[i] = (FT)(1.0 / dgi);
+    }
+    // visible to the solves after the first reduction's barrier
+  }
+
   // registers: x, r (s in the middle of an iteration), p, v, t; r_hat = b is
   // re-read from global memory (L1) and p_hat / s_hat from shared memory
   double x[R], r[R], p[R], v[R], t[R];
@@ -177,8 +273,9 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
     stop = true;
   }
 
-// z = M in for this thread's rows.  The input is in `sin` (sph for PV 0),
-// made visible by a barrier; z lands in sph, followed by a barrier.
+// z = M in for this thread's rows.  The input is in `sin` (sph for PV 0 and
+// for FP64 factors), made visible by a barrier; z lands in sph, followed by a
+// barrier.
 #define BILU_RR_APPLY()                                                                                          \
   do {                                                                                                           \
     if (PV == 1) {                                                                                               \
@@ -203,6 +300,8 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
         if (i < n) sph[i] = (double)z_[k];                                                                       \
       }                                                                                                          \
       __syncthreads();                                                                                           \
+    } else if (PV == 3) {                                                                                        \
+      lu_apply<FT>(P, Fs, rinv, sizeof(FT) == 8 ? reinterpret_cast<FT*>(sph) : sin, sph, tid, nt);              \
     }                                                                                                            \
   } while (0)
 // writes this thread's rows of `vec` as the preconditioner input
@@ -211,7 +310,7 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
     _Pragma("unroll") for (int k = 0; k < R; ++k) { \
       const int i = tid + k * nt;                \
       if (i < n) {                               \
-        if (PV == 0)                             \
+        if (PV == 0 || (PV == 3 && sizeof(FT) == 8)) \
           sph[i] = vec[k];                       \
         else                                     \
           sin[i] = (FT)vec[k];                   \
@@ -386,6 +485,7 @@ int rr_max_threads(int R) { return R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256
 const void* rr_kernel(int pv, int fp32, int R) {
   if (pv == 0) return rr_kernel_pv<0, double>(R);
   if (pv == 1) return fp32 ? rr_kernel_pv<1, float>(R) : rr_kernel_pv<1, double>(R);
+  if (pv == 3) return fp32 ? rr_kernel_pv<3, float>(R) : rr_kernel_pv<3, double>(R);
   return fp32 ? rr_kernel_pv<2, float>(R) : rr_kernel_pv<2, double>(R);
 }
 
@@ -395,6 +495,7 @@ cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int p
   if (R == 0 || nt % 32 || nt > rr_max_threads(R)) return cudaErrorInvalidConfiguration;
   if (pv == 0) return launch_rr_pv<0, double>(a, L, nt, R, st);
   if (pv == 1) return fp32 ? launch_rr_pv<1, float>(a, L, nt, R, st) : launch_rr_pv<1, double>(a, L, nt, R, st);
+  if (pv == 3) return fp32 ? launch_rr_pv<3, float>(a, L, nt, R, st) : launch_rr_pv<3, double>(a, L, nt, R, st);
   return fp32 ? launch_rr_pv<2, float>(a, L, nt, R, st) : launch_rr_pv<2, double>(a, L, nt, R, st);
 }
 

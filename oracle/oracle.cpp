@@ -663,8 +663,32 @@ ORC_API void orc_bicgstab(int n, int nnz, const int* rp, const int* ci, int nsys
 //   block            0.0 + w_0 + w_1 + ... over the warps in order
 //   rows             A*x and the ISAI rows: fma over the row, from 0.0; ISAI in
 //                    float when fp32 (input rounded, output widened)
-// pv: 0 none, 1 z = aiU (aiL v), 2 z = aiA v.  No reference counterpart.
+//   LU solve         in-place factors: input rounded to FT; lower rows ascending,
+//                    s = fma(l_ik, y_k, s) over k ascending from 0, y_i = y_i - s;
+//                    upper rows descending, s = fma(u_ik, z_k, s) over k descending
+//                    from 0, z_i = (y_i - s) * rinv_i, rinv_i = 1.0 / u_ii (FP64,
+//                    rounded to float for FP32 factors); output widened
+// pv: 0 none, 1 z = aiU (aiL v), 2 z = aiA v, 3 z = U^-1 L^-1 v (in-place LU
+// factors on the factor pattern given as the `l` triangle).  No reference
+// counterpart.
 namespace {
+
+// FAST LU solve in FP64: the level-scheduled kernel computes each row from
+// rows finished in earlier levels, so the row-sequential order below gives the
+// same values.
+inline void trsv_lu_fast(int n, const int* rp, const int* ci, const int* diag, const double* lu,
+                         const double* rinv, const double* v, double* y) {
+  for (int i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int k = rp[i]; k < diag[i]; ++k) s = std::fma(lu[k], y[ci[k]], s);
+    y[i] = v[i] - s;
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = 0.0;
+    for (int k = rp[i + 1] - 1; k > diag[i]; --k) s = std::fma(lu[k], y[ci[k]], s);
+    y[i] = (y[i] - s) * rinv[i];
+  }
+}
 
 double fast_block_sum(const std::vector<double>& part, int nt) {
   double s = 0.0;
@@ -702,6 +726,8 @@ ORC_API int orc_bicgstab_fast(int n, int nnz, const int* rp, const int* ci, int 
   if (!R) return -1;
   // bilu.h BILU_SYS_* values
   constexpr int kConverged = 1, kMaxIter = -1, kBreakdown = -2, kNonfinite = -3, kZeroRhs = 2, kInitialOk = 3;
+  std::vector<int> ldiag(pv == 3 ? n : 0);
+  if (pv == 3) orc_find_diag(n, l_rp, l_ci, ldiag.data());
 #pragma omp parallel for schedule(dynamic, 1)
   for (int s = 0; s < nsys; ++s) {
     const double* As = A + (size_t)s * nnz;
@@ -711,8 +737,15 @@ ORC_API int orc_bicgstab_fast(int n, int nnz, const int* rp, const int* ci, int 
     const double* Ud = u_vals ? u_vals + (size_t)s * u_nnz : nullptr;
     const float* Uf = u_vals32 ? u_vals32 + (size_t)s * u_nnz : nullptr;
     std::vector<double> x(n, 0.0), r(bs, bs + n), p(n, 0.0), v(n, 0.0), t(n, 0.0), sph(n, 0.0), part(nt);
-    std::vector<double> ind(n), midd(n);
-    std::vector<float> inf(n), midf(n);
+    std::vector<double> ind(n), midd(n), rinvd(pv == 3 ? n : 0);
+    std::vector<float> inf(n), midf(n), rinvf(pv == 3 ? n : 0);
+    if (pv == 3)
+      for (int i = 0; i < n; ++i) {
+        if (fp32)
+          rinvf[i] = (float)(1.0 / (double)Lf[ldiag[i]]);
+        else
+          rinvd[i] = 1.0 / Ld[ldiag[i]];
+      }
     // per-thread partial sums of f(i) over thread t's rows
     auto reduce = [&](auto f) {
       for (int th = 0; th < nt; ++th) {
@@ -729,6 +762,11 @@ ORC_API int orc_bicgstab_fast(int n, int nnz, const int* rp, const int* ci, int 
     auto apply = [&](const std::vector<double>& in) {
       if (pv == 0) {
         sph = in;
+      } else if (pv == 3) {
+        if (fp32)
+          trsv_lu_f32(n, l_rp, l_ci, ldiag.data(), Lf, rinvf.data(), in.data(), inf.data(), sph.data());
+        else
+          trsv_lu_fast(n, l_rp, l_ci, ldiag.data(), Ld, rinvd.data(), in.data(), sph.data());
       } else if (fp32) {
         for (int i = 0; i < n; ++i) inf[i] = (float)in[i];
         if (pv == 1) {

@@ -196,8 +196,9 @@ def bicgstab(rp, ci, A, b, prec=PREC_LU, lu=None, ail=None, aiu=None, dot=0, tol
 
 def bicgstab_fast(rp, ci, A, b, nt, pv=1, ail=None, aiu=None, fp32=False, tol_mode=0, tol=1e-11, max_iter=500):
     """BILU_REDUCE_FAST order of the register-resident solver with `nt` threads per system.  pv: 0 none,
-    1 ISAI of L and U (ail, aiu = (row_ptrs, col_idxs, values)), 2 general ISAI (ail).  fp32: ISAI values
-    rounded to float and applied in float.  Returns x, iters, conv, res, status, true_res."""
+    1 ISAI of L and U (ail, aiu = (row_ptrs, col_idxs, values)), 2 general ISAI (ail), 3 in-place ILU
+    factors (ail = (factor row_ptrs, col_idxs, LU values)).  fp32: preconditioner values rounded to float
+    and applied in float.  Returns x, iters, conv, res, status, true_res."""
     rp, ci = _ia(rp), _ia(ci)
     A = np.ascontiguousarray(A, np.float64)
     b = np.ascontiguousarray(b, np.float64)

@@ -1,8 +1,10 @@
 """The register-resident FAST solver (csrc/k_solve_rr.cu) against the oracle's
 restatement of its reduction order (orc_bicgstab_fast), bit for bit: ISAI of
-L and U (exact ILU or FAST ParILU factors), general ISAI and no
-preconditioner; FP64 and FP32 ISAI values; several threads-per-system
-choices (1 to 8 rows per thread); edge cases with their status words."""
+L and U (exact ILU or FAST ParILU factors), general ISAI, in-place ILU factors
+(the merged form factorising in the kernel, split ILU(0) approaches and FAST
+ParILU) and no preconditioner; FP64 and FP32 preconditioner values; several
+threads-per-system choices (1 to 8 rows per thread); edge cases with their
+status words."""
 import numpy as np
 import pytest
 
@@ -24,6 +26,12 @@ def _oracle_fast(rp, ci, v, b, precond, nt, fp32, approach=3, sweeps=5, power=2,
         arp, aci = O.isai_pattern(nrp, nci, power)
         ai = O.isai_values(nrp, nci, fv, 2, arp, aci)
         return O.bicgstab_fast(rp, ci, v, b, nt, pv=2, ail=(arp, aci, ai), fp32=fp32, **tol)
+    if precond in (bilu.PRECOND_ILU0, bilu.PRECOND_ILU0_SPLIT, bilu.PRECOND_PARILU0):
+        if precond == bilu.PRECOND_PARILU0:
+            lu = O.parilu0(nrp, nci, fv, sweeps, fast=True)
+        else:
+            lu = O.ilu0(nrp, nci, fv, approach)
+        return O.bicgstab_fast(rp, ci, v, b, nt, pv=3, ail=(nrp, nci, lu), fp32=fp32, **tol)
     if precond == bilu.PRECOND_ILU0_ISAI:
         lu = O.ilu0(nrp, nci, fv, approach)
     else:
@@ -126,3 +134,77 @@ def test_rr_autotuned_plan_bitwise(cuda):
     g = H.gpu_solve(cuda, rp, ci, v, b, threads_per_system=info["threads"], **opts)
     o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_PARILU0_ISAI, info["threads"], True, **TOL)
     _check(g, o, f"autotuned threads {info['threads']}")
+
+
+LU_CASES = [
+    ("2d5_16x16", bilu.PRECOND_ILU0, dict(ilu_approach=1)),
+    ("3d7_7x7x7", bilu.PRECOND_ILU0, dict(ilu_approach=4)),
+    ("cd2d_12x12", bilu.PRECOND_ILU0_SPLIT, dict(ilu_approach=3)),
+    ("3d7_5x5x5", bilu.PRECOND_ILU0_SPLIT, dict(ilu_approach=2)),
+    ("3d7_7x7x7", bilu.PRECOND_PARILU0, dict(parilu_sweeps=4)),
+]
+
+
+@pytest.mark.parametrize("fam,precond,kw", LU_CASES, ids=[f"{c[0]}-p{c[1]}-{list(c[2].values())[0]}" for c in LU_CASES])
+@pytest.mark.parametrize("fp32", [False, True])
+@pytest.mark.parametrize("nt", [0, 64, 128])
+def test_rr_lu_solver_bitwise(cuda, fam, precond, kw, fp32, nt):
+    """In-place ILU factors in shared memory, level-scheduled triangular solves over the CTA."""
+    rp, ci, v, b = H.workload(fam, NSYS)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, reduction=bilu.REDUCE_FAST,
+                    factor_precision=bilu.FP32 if fp32 else bilu.FP64, threads_per_system=nt, **kw, **TOL)
+    used = g["info"]["threads"]
+    if nt:
+        assert used == nt
+    o = _oracle_fast(rp, ci, v, b, precond, used, fp32, approach=kw.get("ilu_approach", 1),
+                     sweeps=kw.get("parilu_sweeps", 5), **TOL)
+    _check(g, o, f"{fam} precond {precond} fp32={fp32} threads={used}")
+    assert np.all(g["conv"] == 1)
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_rr_lu_large_system(cuda, fp32):
+    """n = 1000 (3D 10x10x10): the merged form factorises 6400 entries in shared memory, 128 threads with
+    8 rows each; FP32 factors are rounded in place after the FP64 factorisation."""
+    rp, ci, v, b = bilu.gen_stencil(2, 10, 10, 10, 6, seed=11)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0, reduction=bilu.REDUCE_FAST,
+                    factor_precision=bilu.FP32 if fp32 else bilu.FP64, **TOL)
+    assert g["info"]["threads"] == 128
+    o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_ILU0, 128, fp32, approach=1, **TOL)
+    _check(g, o, f"3D 10x10x10 merged ILU(0) fp32={fp32}")
+
+
+def test_rr_lu_missing_diagonal(cuda):
+    """Split ILU(0) on a pattern without two diagonal entries: the factor pattern has them inserted, A*x
+    keeps the caller's pattern."""
+    rp, ci, v, b = H.workload("2d5_8x8", NSYS)
+    keep = np.ones(len(ci), bool)
+    for row in (5, 40):
+        keep[rp[row] + int(np.where(ci[rp[row]:rp[row + 1]] == row)[0][0])] = False
+    nrp = np.concatenate([[0], np.cumsum([keep[rp[i]:rp[i + 1]].sum() for i in range(len(rp) - 1)])]).astype(np.int32)
+    nci = ci[keep]
+    nv = np.ascontiguousarray(v[:, keep])
+    kw = dict(tol_mode=bilu.TOL_ABS, tol=1e-11, max_iter=20)
+    g = H.gpu_solve(cuda, nrp, nci, nv, b, precond=bilu.PRECOND_ILU0_SPLIT, reduction=bilu.REDUCE_FAST, **kw)
+    assert g["info"]["missing_diag"] == 2
+    o = _oracle_fast(nrp, nci, nv, b, bilu.PRECOND_ILU0_SPLIT, g["info"]["threads"], False, approach=1, **kw)
+    _check(g, o, "missing diagonals, split ILU(0)")
+
+
+def test_rr_lu_edge_cases(cuda):
+    """Merged form: zero right-hand side, one below the threshold from the start, an iteration limit and a
+    NaN in A (non-finite factors)."""
+    rp, ci, v, b = H.workload("2d5_8x8", 6)
+    b = b.copy()
+    v = v.copy()
+    b[1] = 0.0
+    b[2] *= 1e-14
+    v[4, 3] = np.nan
+    for max_iter in (500, 2):
+        kw = dict(tol_mode=bilu.TOL_ABS, tol=1e-11, max_iter=max_iter)
+        g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0, reduction=bilu.REDUCE_FAST, **kw)
+        o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_ILU0, g["info"]["threads"], False, approach=1, **kw)
+        _check(g, o, f"LU edge cases, max_iter {max_iter}")
+        assert g["status"][1] == 2 and g["status"][2] == 3 and g["status"][4] == -3
+        if max_iter == 2:
+            assert g["status"][0] == -1
