@@ -12,6 +12,10 @@
 
 namespace bilu {
 
+// entries per row of a triangular-solve program that the register-resident
+// solver loads one level ahead (the rest it loads when it needs them)
+constexpr int kTrsvPrefetch = 4;
+
 // learned warm start: 9 features -> 64 -> 64 -> 1
 constexpr int kMlpFeatures = 9;
 constexpr int kMlpHidden = 64;
@@ -75,6 +79,15 @@ struct DevPattern {
   int nnz_L = 0, nnz_U = 0;
   const int* l_src = nullptr;
   const int* u_src = nullptr;
+  // triangular-solve programs of the register-resident solver (n <= 1024),
+  // one per triangle.  Level l: header {off, w}; at prog[off + s] the record
+  // of slot s < w, row | count << 10; at prog[off + w + j*w + s] its entry j,
+  // k << 10 | column, in summation order (lower ascending, upper descending k);
+  // every level has at least kTrsvPrefetch entry rows (padding reads as 0).
+  const int2* tp_lo_hdr = nullptr;
+  const int* tp_lo = nullptr;
+  const int2* tp_up_hdr = nullptr;
+  const int* tp_up = nullptr;
   // per row: lower-solve level; per entry: position of the transposed entry or -1
   const int* row_lev = nullptr;
   const int* tpos = nullptr;
@@ -256,6 +269,7 @@ struct bilu_plan {
   std::vector<int> dep;  // pairs
   std::vector<int> l_rp, l_ci, l_src, u_rp, u_ci, u_src;
   std::vector<int> row_lev, tpos, mlp_ent;
+  std::vector<int> tp_lo_hdr, tp_lo, tp_up_hdr, tp_up;  // triangular-solve programs (DevPattern::tp_*)
   std::vector<int> pl_ent;  // ParILU entry classes (see DevPattern::pl_ent)
   int pl_ndep = 0, pl_nlow = 0;
   bool has_isai = false;

@@ -128,6 +128,44 @@ void build_levels(bilu_plan& P) {
                        P.lev_up_ptr, P.lev_up_rows, P.maxw_up);
 }
 
+// Triangular-solve programs (DevPattern::tp_*) from the level schedules; only
+// for n <= 1024 (10-bit rows and columns), the register-resident solver's range.
+void build_trsv_programs(bilu_plan& P) {
+  P.tp_lo_hdr.clear();
+  P.tp_lo.clear();
+  P.tp_up_hdr.clear();
+  P.tp_up.clear();
+  if (P.n > 1024) return;
+  auto build = [&](const std::vector<int>& lptr, const std::vector<int>& lrows, bool upper, std::vector<int>& hdr,
+                   std::vector<int>& prog) {
+    for (int l = 0; l + 1 < (int)lptr.size(); ++l) {
+      const int w = lptr[l + 1] - lptr[l];
+      int maxc = 0;
+      for (int q = lptr[l]; q < lptr[l + 1]; ++q) {
+        const int i = lrows[q];
+        maxc = std::max(maxc, upper ? P.rp[i + 1] - 1 - P.diag[i] : P.diag[i] - P.rp[i]);
+      }
+      const int rows_e = std::max(maxc, bilu::kTrsvPrefetch);
+      const int off = (int)prog.size();
+      hdr.push_back(off);
+      hdr.push_back(w);
+      prog.resize(off + (size_t)w * (1 + rows_e), 0);
+      for (int s = 0; s < w; ++s) {
+        const int i = lrows[lptr[l] + s];
+        int j = 0;
+        if (upper) {
+          for (int k = P.rp[i + 1] - 1; k > P.diag[i]; --k, ++j) prog[off + w + (size_t)j * w + s] = k << 10 | P.ci[k];
+        } else {
+          for (int k = P.rp[i]; k < P.diag[i]; ++k, ++j) prog[off + w + (size_t)j * w + s] = k << 10 | P.ci[k];
+        }
+        prog[off + s] = i | j << 10;
+      }
+    }
+  };
+  build(P.lev_lo_ptr, P.lev_lo_rows, false, P.tp_lo_hdr, P.tp_lo);
+  build(P.lev_up_ptr, P.lev_up_rows, true, P.tp_up_hdr, P.tp_up);
+}
+
 void build_deps(bilu_plan& P) { bilu::pattern_deps(P.n, P.rp.data(), P.ci.data(), P.diag.data(), P.dep_ptr, P.dep); }
 
 // structural pattern of T^power, T given by (trp, tci)
@@ -302,6 +340,7 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   if (pv == 1 || pv == 2 || (pv == 3 && fp32)) take(L.in, (long long)n * fts);
   if (pv == 1) take(L.mid, (long long)n * fts);
   if (pv == 3) {
+    if (P.tp_lo.empty()) return false;
     // the merged form factorises in FP64 in this slot before rounding to FT
     take(L.F, (long long)P.nnz * (pk == PK_ILU_INKERNEL ? 8 : fts));
     take(L.rinv, (long long)n * fts);
@@ -363,6 +402,7 @@ bilu_status upload(bilu_plan& P) {
   const size_t o_lsrc = put(P.l_src), o_usrc = put(P.u_src);
   const size_t o_rlev = put(P.row_lev), o_tpos = put(P.tpos), o_ment = put(P.mlp_ent);
   const size_t o_plent = put(P.pl_ent);
+  const size_t o_tlh = put(P.tp_lo_hdr), o_tl = put(P.tp_lo), o_tuh = put(P.tp_up_hdr), o_tu = put(P.tp_up);
   size_t o_alrp = 0, o_alci = 0, o_aurp = 0, o_auci = 0, o_alpp = 0, o_alp = 0, o_aupp = 0, o_aup = 0;
   size_t o_gmp = 0, o_gm = 0, o_gp = 0;
   if (P.general_isai) {
@@ -417,6 +457,12 @@ bilu_status upload(bilu_plan& P) {
   d.n_mlp = (int)P.mlp_ent.size();
   d.mlp_ent = b + o_ment;
   d.pl_ent = b + o_plent;
+  if (!P.tp_lo.empty()) {
+    d.tp_lo_hdr = reinterpret_cast<const int2*>(b + o_tlh);
+    d.tp_lo = b + o_tl;
+    d.tp_up_hdr = reinterpret_cast<const int2*>(b + o_tuh);
+    d.tp_up = b + o_tu;
+  }
   d.pl_ndep = P.pl_ndep;
   d.pl_nlow = P.pl_nlow;
   if (P.has_isai) {
@@ -604,6 +650,7 @@ bilu_status bilu_plan_create(bilu_plan** out, int n, int nnz, const int* h_rp, c
     P->u_rp[i + 1] = (int)P->u_ci.size();
   }
   build_levels(*P);
+  build_trsv_programs(*P);
   build_deps(*P);
   P->row_lev.assign(n, 0);
   for (int l = 0; l + 1 < (int)P->lev_lo_ptr.size(); ++l)

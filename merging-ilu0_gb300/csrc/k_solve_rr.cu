@@ -108,40 +108,80 @@ __device__ __forceinline__ void rows_acc(const VT* __restrict__ val, const int* 
   }
 }
 
-// z = U^{-1} L^{-1} y over the CTA, level by level, in place on y (the
-// preconditioner input, already rounded to FT).  For FP32 factors the upper
-// solve also widens each z_i into zd (the FP64 SpMV input); for FP64 factors y
-// is that vector.  Ends with a barrier: z is visible to every thread.
+// One triangle of z = U^{-1} L^{-1} y over the CTA, level by level, in place
+// on y, from the triangle's solve program (DevPattern::tp_*).  Thread t takes
+// slot t of every level (and t + nt, ... of wider ones); the record and the
+// first kTrsvPrefetch entries of its next slot are loaded one level ahead and
+// the level headers two levels ahead, so the global-memory latency of the
+// program overlaps the current level's arithmetic and barrier.
+// UPPER: z_i = (y_i - s) * rinv_i, also widened into zd for FP32 factors;
+// lower: y_i = y_i - s.  Ends with a barrier.
+template <bool UPPER, typename FT>
+__device__ __forceinline__ void tri_solve(const int2* __restrict__ hdr, const int* __restrict__ prog, int nlev,
+                                          const FT* __restrict__ F, const FT* __restrict__ rinv, FT* y, double* zd,
+                                          int tid, int nt) {
+  constexpr int PF = kTrsvPrefetch;
+  auto row = [&](int rec, const int (&e)[PF], int off, int w, int s) {
+    const int i = rec & 1023, cnt = rec >> 10;
+    FT acc = FT(0);
+#pragma unroll
+    for (int j = 0; j < PF; ++j)
+      if (j < cnt) acc = fma_t(F[e[j] >> 10], y[e[j] & 1023], acc);
+    for (int j = PF; j < cnt; ++j) {
+      const int en = __ldg(prog + off + w + j * w + s);
+      acc = fma_t(F[en >> 10], y[en & 1023], acc);
+    }
+    if (UPPER) {
+      const FT z = (y[i] - acc) * rinv[i];
+      y[i] = z;
+      if (sizeof(FT) == 4) zd[i] = (double)z;
+    } else {
+      y[i] = y[i] - acc;
+    }
+  };
+  auto fetch = [&](int2 h, int& rec, int (&e)[PF]) {
+    rec = 0;
+    if (tid < h.y) {
+      rec = __ldg(prog + h.x + tid);
+#pragma unroll
+      for (int j = 0; j < PF; ++j) e[j] = __ldg(prog + h.x + h.y + j * h.y + tid);
+    }
+  };
+  const int2 zero = make_int2(0, 0);
+  int2 h = nlev > 0 ? __ldg(hdr) : zero;
+  int2 hn = nlev > 1 ? __ldg(hdr + 1) : zero;
+  int rec, e[PF];
+  fetch(h, rec, e);
+  for (int lev = 0; lev < nlev; ++lev) {
+    const int2 hnn = lev + 2 < nlev ? __ldg(hdr + lev + 2) : zero;
+    int recn, en[PF];
+    fetch(hn, recn, en);
+    if (tid < h.y) row(rec, e, h.x, h.y, tid);
+    for (int s = tid + nt; s < h.y; s += nt) {
+      int r2, e2[PF];
+      r2 = __ldg(prog + h.x + s);
+#pragma unroll
+      for (int j = 0; j < PF; ++j) e2[j] = __ldg(prog + h.x + h.y + j * h.y + s);
+      row(r2, e2, h.x, h.y, s);
+    }
+    __syncthreads();
+    h = hn;
+    hn = hnn;
+    rec = recn;
+#pragma unroll
+    for (int j = 0; j < PF; ++j) e[j] = en[j];
+  }
+}
+
+// z = U^{-1} L^{-1} y over the CTA (y: the preconditioner input, already
+// rounded to FT; for FP64 factors y is the FP64 SpMV input itself, for FP32
+// factors the upper solve widens z into zd).  Ends with a barrier: z is
+// visible to every thread.
 template <typename FT>
 __device__ __forceinline__ void lu_apply(const DevPattern& P, const FT* __restrict__ F, const FT* __restrict__ rinv,
                                          FT* y, double* zd, int tid, int nt) {
-  const int* __restrict__ rp = P.rp;
-  const int* __restrict__ ci = P.ci;
-  const int* __restrict__ dg = P.diag;
-  for (int lev = 0; lev < P.nlev_lo; ++lev) {
-    const int b = __ldg(P.lev_lo_ptr + lev), e = __ldg(P.lev_lo_ptr + lev + 1);
-    for (int q = b + tid; q < e; q += nt) {
-      const int i = __ldg(P.lev_lo_rows + q);
-      const int beg = __ldg(rp + i), d = __ldg(dg + i);
-      FT s = FT(0);
-      for (int k = beg; k < d; ++k) s = fma_t(F[k], y[__ldg(ci + k)], s);
-      y[i] = y[i] - s;
-    }
-    __syncthreads();
-  }
-  for (int lev = 0; lev < P.nlev_up; ++lev) {
-    const int b = __ldg(P.lev_up_ptr + lev), e = __ldg(P.lev_up_ptr + lev + 1);
-    for (int q = b + tid; q < e; q += nt) {
-      const int i = __ldg(P.lev_up_rows + q);
-      const int end = __ldg(rp + i + 1), d = __ldg(dg + i);
-      FT s = FT(0);
-      for (int k = end - 1; k > d; --k) s = fma_t(F[k], y[__ldg(ci + k)], s);
-      const FT z = (y[i] - s) * rinv[i];
-      y[i] = z;
-      if (sizeof(FT) == 4) zd[i] = (double)z;
-    }
-    __syncthreads();
-  }
+  tri_solve<false>(P.tp_lo_hdr, P.tp_lo, P.nlev_lo, F, rinv, y, zd, tid, nt);
+  tri_solve<true>(P.tp_up_hdr, P.tp_up, P.nlev_up, F, rinv, y, zd, tid, nt);
 }
 
 // PV: 0 none, 1 ISAI of L and U (z = aiU (aiL v)), 2 general ISAI (z = aiA v),
