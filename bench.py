@@ -45,13 +45,22 @@ SECONDARY = [
          desc="headline workload with FP64 ISAI values",
          opts=dict(precond=4, parilu_sweeps=5, isai_power=2, tol_mode=1, tol=1e-10, reduction=1, factor_precision=0)),
     dict(name="plain_ilu0_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096,
-         desc="plain form on the headline systems: merged FP64 ILU(0) BiCGSTAB (shared-memory kernel), FAST order",
+         desc="plain form on the headline systems: merged FP64 ILU(0) BiCGSTAB, FAST order (register-resident "
+              "kernel: ILU(0) and the factors in shared memory, vectors in registers)",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1)),
+    dict(name="fp32_ilu0_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096,
+         desc="headline systems, merged ILU(0) with the factors stored and applied in FP32 (FP64 factorisation, "
+              "A*x, inner products, recurrences), FAST order",
+         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1), fwd_sample=32),
     dict(name="plain_ilu0_2d5_16x16_fast", kind=1, grid=(16, 16, 1), nsys=16384,
-         desc="plain form: merged ILU(0) BiCGSTAB, 16384 FP64 systems, 2D 5-point 16x16, rel 1e-10, FAST order",
+         desc="plain form: merged FP64 ILU(0) BiCGSTAB, 16384 FP64 systems, 2D 5-point 16x16, rel 1e-10, FAST order "
+              "(register-resident kernel)",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1)),
+    dict(name="fp32_ilu0_2d5_16x16", kind=1, grid=(16, 16, 1), nsys=16384,
+         desc="16384 2D 5-point 16x16 systems, merged ILU(0) with FP32-stored factors, FAST order",
+         opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1)),
     dict(name="plain_ilu0_2d5_16x16_ref", kind=1, grid=(16, 16, 1), nsys=16384,
-         desc="plain form in the reference's operation order (bit-identical iterates)",
+         desc="plain form in the reference's operation order (bit-identical iterates; shared-memory kernel)",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=0)),
     dict(name="fp32_isai_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768, autotune=True,
          desc="ILU(0) + ISAI stored and applied in FP32 (FP64 A*x, inner products, recurrences), 32768 "
@@ -501,13 +510,32 @@ def main():
     if rank != 0:
         return
     chosen = {}
+    by_name = {sc.get("name"): sc for sc in secondary if "systems_per_s" in sc}
+    plain = by_name.get("plain_ilu0_3d7_10x10x10")
+    if plain:
+        # FP64 operations of the plain form: A*x, two triangular solves on the in-place factors (nnz entries),
+        # inner products and vector updates per iteration
+        pfl = fp64_flops_per_iter(res["n"], res["nnz"], res["nnz"], 0) * plain["mean_iters"] * plain["nsys"]
+        chosen["headline_3d7_10x10x10"] = {
+            "workload": HEADLINE["desc"], "plain_form": "merged FP64 ILU(0) + BiCGSTAB on the same systems",
+            "plain_systems_per_s": plain["systems_per_s"],
+            "plain_roofline_fp64_frac": pfl / (plain["solve_ms"] / 1e3) / 1e9 / 1205.0,
+            "chosen_form": "ParILU(5) + ISAI stored and applied in FP32, register-resident solver",
+            "chosen_systems_per_s": res["systems_per_s"], "ratio": res["systems_per_s"] / plain["systems_per_s"]}
+        f32 = by_name.get("fp32_ilu0_3d7_10x10x10")
+        if f32:
+            chosen["fp32_factors_3d7_10x10x10"] = {
+                "workload": "the headline systems", "plain_form": "merged FP64 ILU(0) + BiCGSTAB",
+                "plain_systems_per_s": plain["systems_per_s"],
+                "chosen_form": "merged ILU(0), factors stored and applied in FP32",
+                "chosen_systems_per_s": f32["systems_per_s"], "ratio": f32["systems_per_s"] / plain["systems_per_s"]}
+    p16, f16 = by_name.get("plain_ilu0_2d5_16x16_fast"), by_name.get("fp32_ilu0_2d5_16x16")
+    if p16 and f16:
+        chosen["fp32_factors_2d5_16x16"] = {
+            "workload": "16384 2D 5-point 16x16 systems", "plain_form": "merged FP64 ILU(0) + BiCGSTAB",
+            "plain_systems_per_s": p16["systems_per_s"], "chosen_form": "merged ILU(0), FP32-stored factors",
+            "chosen_systems_per_s": f16["systems_per_s"], "ratio": f16["systems_per_s"] / p16["systems_per_s"]}
     for sc in secondary:
-        if sc.get("name") == "plain_ilu0_3d7_10x10x10" and "systems_per_s" in sc:
-            chosen["headline_3d7_10x10x10"] = {
-                "workload": HEADLINE["desc"], "plain_form": "merged FP64 ILU(0) + BiCGSTAB on the same systems",
-                "plain_systems_per_s": sc["systems_per_s"],
-                "chosen_form": "ParILU(5) + ISAI stored and applied in FP32, register-resident solver",
-                "chosen_systems_per_s": res["systems_per_s"], "ratio": res["systems_per_s"] / sc["systems_per_s"]}
         if sc.get("name") == "learned_warm_start_3d7_7x7x7" and "learned" in sc:
             chosen["learned_3d7_7x7x7"] = {
                 "workload": "16384 fresh 3D 7-point 7x7x7 systems (n=343), rel. tol 1e-10",
