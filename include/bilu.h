@@ -106,7 +106,10 @@ typedef struct bilu_options {
   int    smem_staging;       /* register-resident solver only: -1 automatic; else a bit mask
                                 of the operands copied to shared memory once per system
                                 (bit 0: A, bit 1: aiL / aiA, bit 2: aiU), the rest read
-                                through L1.  Operands that do not fit are left out.       */
+                                through L1.  Operands that do not fit are left out.
+                                Bit 3: A and aiU left in global memory are read from
+                                SELL-32 copies made before the solver launch (same
+                                arithmetic; the copies live in the plan's workspace).     */
 } bilu_options;
 
 /* Fills *opts with the reference defaults: merged ILU(0), approach 1, 5 sweeps,
@@ -206,7 +209,8 @@ bilu_status bilu_plan_last_timing(bilu_plan* plan, bilu_timing* timing);
 
 /* Times the register-resident solver's configurations on this batch -- threads
  * per system 1x, 2x and 4x the fewest that give 8 rows per thread, shared-memory
- * staging of none / aiL / aiL + aiU / A -- and keeps the fastest for the plan's
+ * staging of none / aiL / aiL + aiU / A, SELL-32 copies of the operands left in
+ * global memory or not -- and keeps the fastest for the plan's
  * later solves.  Plans that do not use that solver (bilu_plan_info.solver_kernel
  * 0) are left unchanged.  Runs full solves of the batch (d_x is overwritten) and
  * synchronises.  No reference counterpart. */

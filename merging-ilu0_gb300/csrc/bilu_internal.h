@@ -88,6 +88,17 @@ struct DevPattern {
   const int* tp_lo = nullptr;
   const int2* tp_up_hdr = nullptr;
   const int* tp_up = nullptr;
+  // SELL-32 copies for the register-resident solver's SpMVs, of A (sa_*) and of
+  // aiU (su_*): slice s holds rows 32s .. 32s+31, entry j of row 32s+l at
+  // off[s] + 32j + l, so a warp's 32 rows read one contiguous line per entry;
+  // src = the CSR position each SELL position copies (-1: padding, never read)
+  int sa_nnz = 0, su_nnz = 0;
+  const int* sa_off = nullptr;
+  const int* sa_ci = nullptr;
+  const int* sa_src = nullptr;
+  const int* su_off = nullptr;
+  const int* su_ci = nullptr;
+  const int* su_src = nullptr;
   // per row: lower-solve level; per entry: position of the transposed entry or -1
   const int* row_lev = nullptr;
   const int* tpos = nullptr;
@@ -131,6 +142,8 @@ struct SolveArgs {
   const double* A = nullptr;   // nsys*a_nnz, operator (caller's) pattern
   const double* b = nullptr;
   double* x = nullptr;
+  const double* A_sell = nullptr;  // A in the SELL-32 layout (register-resident solver; null: CSR)
+  const void* aiu_sell = nullptr;  // aiU in the SELL-32 layout (register-resident solver; null: CSR)
   const void* F = nullptr;     // PK_LU_GLOBAL factors (double or float)
   const void* ail = nullptr;   // PK_ISAI
   const void* aiu = nullptr;
@@ -248,6 +261,10 @@ cudaError_t launch_mlp_warm(const DevPattern& p, int nsys, const double* A, cons
                             const float* corr, const void* pbf, double threshold, double* lu0, double* res, int* used,
                             cudaStream_t st);
 cudaError_t launch_to_float(const double* a, float* b, size_t n, cudaStream_t st);
+// out[s][p] = in[s][src[p]] (0 where src[p] < 0) for nsys systems of csr_nnz
+// values into sell_nnz positions; elem_bytes 8 (double) or 4 (float)
+cudaError_t launch_to_sell(const int* src, int sell_nnz, int csr_nnz, int nsys, const void* in, void* out,
+                           int elem_bytes, cudaStream_t st);
 cudaError_t launch_isai_general(const DevPattern& p, int nsys, const double* A, void* ai, int fp32, int threads,
                                 cudaStream_t st);
 cudaError_t launch_split(const DevPattern& p, int nsys, const double* lu, double* L, double* U, cudaStream_t st);
@@ -270,6 +287,7 @@ struct bilu_plan {
   std::vector<int> l_rp, l_ci, l_src, u_rp, u_ci, u_src;
   std::vector<int> row_lev, tpos, mlp_ent;
   std::vector<int> tp_lo_hdr, tp_lo, tp_up_hdr, tp_up;  // triangular-solve programs (DevPattern::tp_*)
+  std::vector<int> sa_off, sa_ci, sa_src, su_off, su_ci, su_src;  // SELL-32 layouts (DevPattern::sa_*, su_*)
   std::vector<int> pl_ent;  // ParILU entry classes (see DevPattern::pl_ent)
   int pl_ndep = 0, pl_nlow = 0;
   bool has_isai = false;
@@ -285,6 +303,7 @@ struct bilu_plan {
   // register-resident FAST solver (k_solve_rr.cu), when it applies
   bool rr = false;
   int rr_threads = 0, rr_pv = 0;
+  bool rr_sell = false;  // SpMVs read SELL-32 copies of A (and of aiU) made before the solver launch
   bilu::RRLayout rr_lay;
   // workspace
   void* ws = nullptr;

@@ -166,6 +166,31 @@ void build_trsv_programs(bilu_plan& P) {
   build(P.lev_up_ptr, P.lev_up_rows, true, P.tp_up_hdr, P.tp_up);
 }
 
+// SELL-32 layout of a pattern with n <= 1024 rows (DevPattern::sa_* / su_*).
+void build_sell(int n, const std::vector<int>& rp, const std::vector<int>& ci, std::vector<int>& off,
+                std::vector<int>& sci, std::vector<int>& src) {
+  off.clear();
+  sci.clear();
+  src.clear();
+  if (n > 1024 || rp.empty()) return;
+  const int ns = (n + 31) / 32;
+  off.assign(ns + 1, 0);
+  for (int s = 0; s < ns; ++s) {
+    int w = 0;
+    for (int i = 32 * s; i < std::min(n, 32 * s + 32); ++i) w = std::max(w, rp[i + 1] - rp[i]);
+    off[s + 1] = off[s] + 32 * w;
+  }
+  sci.assign(off[ns], 0);
+  src.assign(off[ns], -1);
+  for (int i = 0; i < n; ++i) {
+    const int base = off[i / 32] + (i % 32);
+    for (int k = rp[i]; k < rp[i + 1]; ++k) {
+      sci[base + 32 * (k - rp[i])] = ci[k];
+      src[base + 32 * (k - rp[i])] = k;
+    }
+  }
+}
+
 void build_deps(bilu_plan& P) { bilu::pattern_deps(P.n, P.rp.data(), P.ci.data(), P.diag.data(), P.dep_ptr, P.dep); }
 
 // structural pattern of T^power, T given by (trp, tci)
@@ -315,7 +340,8 @@ void choose_layout(bilu_plan& P) {
 // 8 rows per thread.  rr_configure sets the plan up for `nt` threads per system
 // and the shared-memory staging `mask` (bit 0 A, bit 1 aiL / aiA, bit 2 aiU;
 // operands that would cost occupancy are left in global memory, read through
-// L1; ILU factors are always staged); false when the kernel does not apply or
+// L1; ILU factors are always staged; bit 3: the SpMVs read SELL-32 copies of
+// the operands left in global memory); false when the kernel does not apply or
 // that configuration is invalid.
 bool rr_configure(bilu_plan& P, int nt, int mask) {
   const bilu_options& o = P.opts;
@@ -369,20 +395,24 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   P.rr_threads = nt;
   P.rr_pv = pv;
   P.rr_lay = L;
+  P.rr_sell = (mask & 8) != 0 && !P.sa_off.empty();
   return true;
 }
 
 // Default: the caller's threads per system, else the fewest warps that give
 // every thread at most 8 rows (one warp for n <= 256); the caller's staging
-// mask, else the ISAI values but not A.  Measured on GB300 (3D 7-point
-// 10x10x10, 7x7x7, 2D 16x16): A read through L1 beats A in shared memory, whose
-// carve-out shrinks the L1 left for the column indices and ISAI values; the
-// FP32 aiL in shared memory helps when it fits.
+// mask, else the ISAI values but not A; SELL-32 copies for ILU factors at
+// n > 512.  Measured on GB300 (3D 7-point 10x10x10, 7x7x7, 2D 16x16): A read
+// through L1 beats A in shared memory, whose carve-out shrinks the L1 left for
+// the column indices and ISAI values; the FP32 aiL in shared memory helps when
+// it fits; the SELL-32 copy of A gains 5 % with ILU factors at 10x10x10
+// (128 threads) and loses up to 6 % on the smaller systems and with ISAI.
 void choose_rr(bilu_plan& P) {
   const bilu_options& o = P.opts;
   P.rr = false;
   const int nt = o.threads_per_system > 0 ? o.threads_per_system : round_up((P.n + 7) / 8, 32);
-  rr_configure(P, nt, o.smem_staging >= 0 ? o.smem_staging : 6);
+  const bool lu = prec_kind(o.precond) == PK_ILU_INKERNEL || prec_kind(o.precond) == PK_LU_GLOBAL;
+  rr_configure(P, nt, o.smem_staging >= 0 ? o.smem_staging : (6 | (lu && P.n > 512 ? 8 : 0)));
 }
 
 bilu_status upload(bilu_plan& P) {
@@ -403,6 +433,8 @@ bilu_status upload(bilu_plan& P) {
   const size_t o_rlev = put(P.row_lev), o_tpos = put(P.tpos), o_ment = put(P.mlp_ent);
   const size_t o_plent = put(P.pl_ent);
   const size_t o_tlh = put(P.tp_lo_hdr), o_tl = put(P.tp_lo), o_tuh = put(P.tp_up_hdr), o_tu = put(P.tp_up);
+  const size_t o_sao = put(P.sa_off), o_sac = put(P.sa_ci), o_sas = put(P.sa_src);
+  const size_t o_suo = put(P.su_off), o_suc = put(P.su_ci), o_sus = put(P.su_src);
   size_t o_alrp = 0, o_alci = 0, o_aurp = 0, o_auci = 0, o_alpp = 0, o_alp = 0, o_aupp = 0, o_aup = 0;
   size_t o_gmp = 0, o_gm = 0, o_gp = 0;
   if (P.general_isai) {
@@ -457,6 +489,18 @@ bilu_status upload(bilu_plan& P) {
   d.n_mlp = (int)P.mlp_ent.size();
   d.mlp_ent = b + o_ment;
   d.pl_ent = b + o_plent;
+  if (!P.sa_off.empty()) {
+    d.sa_nnz = P.sa_off.back();
+    d.sa_off = b + o_sao;
+    d.sa_ci = b + o_sac;
+    d.sa_src = b + o_sas;
+  }
+  if (!P.su_off.empty()) {
+    d.su_nnz = P.su_off.back();
+    d.su_off = b + o_suo;
+    d.su_ci = b + o_suc;
+    d.su_src = b + o_sus;
+  }
   if (!P.tp_lo.empty()) {
     d.tp_lo_hdr = reinterpret_cast<const int2*>(b + o_tlh);
     d.tp_lo = b + o_tl;
@@ -517,7 +561,7 @@ bilu_status check_opts(const bilu_options* o) {
     return set_error(BILU_ERR_INVALID, "options: threads_per_system must be 0..1024");
   if (!(o->parilu_res_tol >= 0.0)) return set_error(BILU_ERR_INVALID, "options: parilu_res_tol must be >= 0");
   if (o->isai_lower_diag != 0 && o->isai_lower_diag != 1) return set_error(BILU_ERR_INVALID, "options: isai_lower_diag");
-  if (o->smem_staging < -1 || o->smem_staging > 7) return set_error(BILU_ERR_INVALID, "options: smem_staging must be -1..7");
+  if (o->smem_staging < -1 || o->smem_staging > 15) return set_error(BILU_ERR_INVALID, "options: smem_staging must be -1..15");
   return BILU_OK;
 }
 
@@ -688,6 +732,8 @@ bilu_status bilu_plan_create(bilu_plan** out, int n, int nnz, const int* h_rp, c
       return st;
     }
   }
+  build_sell(n, P->in_rp, P->in_ci, P->sa_off, P->sa_ci, P->sa_src);
+  if (P->has_isai && !P->general_isai) build_sell(n, P->aiu_rp, P->aiu_ci, P->su_off, P->su_ci, P->su_src);
   choose_layout(*P);
   choose_rr(*P);
   if (!P->rr && P->lay.total > (int)solve_max_smem()) {
@@ -739,10 +785,11 @@ bilu_status bilu_plan_autotune(bilu_plan* P, int nsys, const double* d_values, c
   const int base = round_up((P->n + 7) / 8, 32);
   const int keep_nt = P->rr_threads;
   const RRLayout keep_lay = P->rr_lay;
+  const bool keep_sell = P->rr_sell;
   float best = -1.0f;
   int best_nt = keep_nt, best_mask = -1;
   for (int f : {1, 2, 4}) {
-    for (int mask : {0, 2, 6, 1}) {
+    for (int mask : {0, 2, 6, 1, 8, 10, 14}) {
       if (!rr_configure(*P, base * f, mask)) continue;
       float ms = 0.0f;
       for (int rep = 0; rep < 2; ++rep) {  // the first run warms caches; the second is timed
@@ -767,6 +814,7 @@ bilu_status bilu_plan_autotune(bilu_plan* P, int nsys, const double* d_values, c
   } else {
     P->rr_threads = keep_nt;
     P->rr_lay = keep_lay;
+    P->rr_sell = keep_sell;
   }
   P->timing = had_timing;
   return st;
@@ -872,9 +920,17 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
   if (P->has_isai) need += align_up((size_t)P->dp.ail_nnz * nsys * 8);
   const size_t off_aiu = need;
   if (P->has_isai) need += align_up((size_t)P->dp.aiu_nnz * nsys * 8);
+  // SELL-32 copies read by the register-resident solver: A unless it is staged in shared memory,
+  // aiU of the two-triangle ISAI unless staged
+  const bool sell_a = P->rr && P->rr_sell && P->rr_lay.A < 0 && P->dp.sa_nnz > 0;
+  const bool sell_u = P->rr && P->rr_sell && P->rr_pv == 1 && P->rr_lay.aiu < 0 && P->dp.su_nnz > 0;
+  const size_t off_asell = need;
+  if (sell_a) need += align_up((size_t)P->dp.sa_nnz * nsys * 8);
+  const size_t off_usell = need;
+  if (sell_u) need += align_up((size_t)P->dp.su_nnz * nsys * (fp32 ? 4 : 8));
   const int prec = o.precond;
   if (P->timing) cudaEventRecord(P->ev[0], st);
-  if (prec != BILU_PRECOND_ILU0 && prec != BILU_PRECOND_NONE) {
+  if ((prec != BILU_PRECOND_ILU0 && prec != BILU_PRECOND_NONE) || sell_a) {
     bilu_status s = ensure_ws(P, need);
     if (s) return s;
   }
@@ -951,6 +1007,16 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
     }
   }
   if (P->timing) cudaEventRecord(P->ev[1], st);
+  if (sell_u) {
+    e = launch_to_sell(P->dp.su_src, P->dp.su_nnz, P->dp.aiu_nnz, nsys, a.aiu, ws + off_usell, fp32 ? 4 : 8, st);
+    if (e != cudaSuccess) return cuda_err(e, "SELL copy of aiU");
+    a.aiu_sell = ws + off_usell;
+  }
+  if (sell_a) {
+    e = launch_to_sell(P->dp.sa_src, P->dp.sa_nnz, P->dp.a_nnz, nsys, vals, ws + off_asell, 8, st);
+    if (e != cudaSuccess) return cuda_err(e, "SELL copy of A");
+    a.A_sell = (const double*)(ws + off_asell);
+  }
   e = P->rr ? launch_solve_rr(a, P->rr_lay, P->rr_threads, P->rr_pv, fp32 ? 1 : 0, st)
             : launch_solve(a, P->threads, fp32 ? 1 : 0, o.reduction == BILU_REDUCE_FAST ? 1 : 0, maxl, st);
   if (e != cudaSuccess) return cuda_err(e, "solver launch");

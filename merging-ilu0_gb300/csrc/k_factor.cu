@@ -384,6 +384,17 @@ __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, 
     b[i] = (float)a[i];
 }
 
+template <typename T>
+__global__ void k_to_sell(const int* __restrict__ src, int sell_nnz, int csr_nnz, size_t total,
+                          const T* __restrict__ in, T* __restrict__ out) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const size_t s = q / sell_nnz;
+    const int p = (int)(q - s * sell_nnz);
+    const int c = __ldg(src + p);
+    out[q] = c >= 0 ? in[s * csr_nnz + c] : T(0);
+  }
+}
+
 int grid_for(size_t total, int threads) {
   size_t g = (total + threads - 1) / threads;
   if (g > 65536) g = 65536;
@@ -431,6 +442,19 @@ cudaError_t launch_isai(const DevPattern& p, int nsys, const double* lu, void* a
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<DevPattern*>(&p), &nsys, &lu, &ail, &aiu};
   return cudaLaunchKernel(k, dim3(nsys), dim3(threads), args, (size_t)smem, st);
+}
+
+cudaError_t launch_to_sell(const int* src, int sell_nnz, int csr_nnz, int nsys, const void* in, void* out,
+                           int elem_bytes, cudaStream_t st) {
+  const size_t total = (size_t)sell_nnz * nsys;
+  if (total == 0) return cudaSuccess;
+  if (elem_bytes == 8)
+    k_to_sell<double><<<grid_for(total, 256), 256, 0, st>>>(src, sell_nnz, csr_nnz, total,
+                                                           static_cast<const double*>(in), static_cast<double*>(out));
+  else
+    k_to_sell<float><<<grid_for(total, 256), 256, 0, st>>>(src, sell_nnz, csr_nnz, total,
+                                                          static_cast<const float*>(in), static_cast<float*>(out));
+  return cudaGetLastError();
 }
 
 cudaError_t launch_to_float(const double* a, float* b, size_t n, cudaStream_t st) {

@@ -40,11 +40,11 @@
 //   block            s = 0.0; s = s + w_j for warps j = 0 .. NT/32-1
 //   SpMV row         acc = fma(a_k, x_ci(k), acc), k ascending, from 0.0 (FP64)
 //   ISAI row (FT)    the same in FT; input rounded to FT, output widened to FP64
-//   LU solve (FT)    input rounded to FT; lower row i: s = fma(l_ik, y_k, s) over
-//                    k ascending from 0, y_i = y_i - s; upper row i: s = fma(u_ik,
-//                    z_k, s) over k descending from 0, z_i = (y_i - s) * rinv_i
-//                    with rinv_i = 1.0 / u_ii in FP64 (rounded to float for FP32
-//                    factors); z widened to FP64
+//   LU solve (FT)    input rounded to FT; lower row i: a = y_i, a = fma(-l_ik, y_k, a)
+//                    over k ascending, y_i = a; upper row i: a = y_i, a = fma(-u_ik,
+//                    z_k, a) over k descending, z_i = a * rinv_i with rinv_i =
+//                    1.0 / u_ii in FP64 (rounded to float for FP32 factors); z
+//                    widened to FP64
 #include <cuda_runtime.h>
 
 #include "bilu_internal.h"
@@ -108,14 +108,40 @@ __device__ __forceinline__ void rows_acc(const VT* __restrict__ val, const int* 
   }
 }
 
+// rows_acc on a matrix in the SELL-32 layout (DevPattern::sa_* / su_*): the
+// same FMAs in the same order; entry j of the warp's 32 rows (tid + k*nt for
+// one k: 32 consecutive rows, one slice) is one contiguous line of values and
+// of column indices.
+template <int R, typename VT, typename XT>
+__device__ __forceinline__ void rows_acc_sell(const VT* __restrict__ val, const int* __restrict__ sci,
+                                              const int* __restrict__ soff, const int* __restrict__ rp, int tid,
+                                              int nt, int n, const XT* __restrict__ xv, XT (&out)[R]) {
+  int pos[R], len[R];
+  int jmax = 0;
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int i = tid + k * nt;
+    pos[k] = i < n ? __ldg(soff + (i >> 5)) + (i & 31) : 0;
+    len[k] = i < n ? __ldg(rp + i + 1) - __ldg(rp + i) : 0;
+    jmax = max(jmax, len[k]);
+    out[k] = XT(0);
+  }
+  for (int j = 0; j < jmax; ++j) {
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+      if (j < len[k]) out[k] = fma_t((XT)val[pos[k] + 32 * j], xv[__ldg(sci + pos[k] + 32 * j)], out[k]);
+  }
+}
+
 // One triangle of z = U^{-1} L^{-1} y over the CTA, level by level, in place
 // on y, from the triangle's solve program (DevPattern::tp_*).  Thread t takes
 // slot t of every level (and t + nt, ... of wider ones); the record and the
 // first kTrsvPrefetch entries of its next slot are loaded one level ahead and
 // the level headers two levels ahead, so the global-memory latency of the
 // program overlaps the current level's arithmetic and barrier.
-// UPPER: z_i = (y_i - s) * rinv_i, also widened into zd for FP32 factors;
-// lower: y_i = y_i - s.  Ends with a barrier.
+// Row i starts from y_i and subtracts its products in program order (one FMA
+// each, no separate subtraction); UPPER then scales by rinv_i and also widens
+// z_i into zd for FP32 factors.  Ends with a barrier.
 template <bool UPPER, typename FT>
 __device__ __forceinline__ void tri_solve(const int2* __restrict__ hdr, const int* __restrict__ prog, int nlev,
                                           const FT* __restrict__ F, const FT* __restrict__ rinv, FT* y, double* zd,
@@ -123,20 +149,20 @@ __device__ __forceinline__ void tri_solve(const int2* __restrict__ hdr, const in
   constexpr int PF = kTrsvPrefetch;
   auto row = [&](int rec, const int (&e)[PF], int off, int w, int s) {
     const int i = rec & 1023, cnt = rec >> 10;
-    FT acc = FT(0);
+    FT acc = y[i];
 #pragma unroll
     for (int j = 0; j < PF; ++j)
-      if (j < cnt) acc = fma_t(F[e[j] >> 10], y[e[j] & 1023], acc);
+      if (j < cnt) acc = fma_t(-F[e[j] >> 10], y[e[j] & 1023], acc);
     for (int j = PF; j < cnt; ++j) {
       const int en = __ldg(prog + off + w + j * w + s);
-      acc = fma_t(F[en >> 10], y[en & 1023], acc);
+      acc = fma_t(-F[en >> 10], y[en & 1023], acc);
     }
     if (UPPER) {
-      const FT z = (y[i] - acc) * rinv[i];
+      const FT z = acc * rinv[i];
       y[i] = z;
       if (sizeof(FT) == 4) zd[i] = (double)z;
     } else {
-      y[i] = y[i] - acc;
+      y[i] = acc;
     }
   };
   auto fetch = [&](int2 h, int& rec, int (&e)[PF]) {
@@ -212,6 +238,8 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
     for (int k = tid; k < P.a_nnz; k += nt) s[k] = __ldg(Ag + k);
     Am = s;
   }
+  // A in the SELL-32 layout when the caller converted it and it is not staged
+  const double* Asell = (L.A < 0 && a.A_sell) ? a.A_sell + (size_t)sys * P.sa_nnz : nullptr;
   const FT* AIL = nullptr;
   const FT* AIU = nullptr;
   if (PV != 0) {
@@ -234,6 +262,8 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
       AIU = g;
     }
   }
+  const FT* AIUsell =
+      (PV == 1 && L.aiu < 0 && a.aiu_sell) ? reinterpret_cast<const FT*>(a.aiu_sell) + (size_t)sys * P.su_nnz : nullptr;
 
   FT* Fs = nullptr;
   FT* rinv = nullptr;
@@ -326,7 +356,10 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
         if (i < n) smid[i] = z_[k];                                                                              \
       }                                                                                                          \
       __syncthreads();                                                                                           \
-      rows_acc<R>(AIU, P.aiu_ci, P.aiu_rp, tid, nt, n, smid, z_);                                                \
+      if (AIUsell)                                                                                               \
+        rows_acc_sell<R>(AIUsell, P.su_ci, P.su_off, P.aiu_rp, tid, nt, n, smid, z_);                            \
+      else                                                                                                       \
+        rows_acc<R>(AIU, P.aiu_ci, P.aiu_rp, tid, nt, n, smid, z_);                                              \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
         const int i = tid + k * nt;                                                                              \
         if (i < n) sph[i] = (double)z_[k];                                                                       \
@@ -371,7 +404,10 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
     __syncthreads();
     BILU_RR_APPLY();  // p_hat in sph
     // v = A p_hat, (r_hat, v)
-    rows_acc<R>(Am, aci, arp, tid, nt, n, sph, v);
+    if (Asell)
+      rows_acc_sell<R>(Asell, P.sa_ci, P.sa_off, arp, tid, nt, n, sph, v);
+    else
+      rows_acc<R>(Am, aci, arp, tid, nt, n, sph, v);
     q[0] = 0.0;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -403,7 +439,10 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
     }
     BILU_RR_APPLY();  // s_hat in sph
     // t = A s_hat, (t, s), (t, t)
-    rows_acc<R>(Am, aci, arp, tid, nt, n, sph, t);
+    if (Asell)
+      rows_acc_sell<R>(Asell, P.sa_ci, P.sa_off, arp, tid, nt, n, sph, t);
+    else
+      rows_acc<R>(Am, aci, arp, tid, nt, n, sph, t);
     double q2[2] = {0.0, 0.0};
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -468,7 +507,10 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
     }
     __syncthreads();
     double ax[R];
-    rows_acc<R>(Am, aci, arp, tid, nt, n, sph, ax);
+    if (Asell)
+      rows_acc_sell<R>(Asell, P.sa_ci, P.sa_off, arp, tid, nt, n, sph, ax);
+    else
+      rows_acc<R>(Am, aci, arp, tid, nt, n, sph, ax);
     q[0] = 0.0;
 #pragma unroll
     for (int k = 0; k < R; ++k) {

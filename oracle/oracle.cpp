@@ -664,29 +664,29 @@ ORC_API void orc_bicgstab(int n, int nnz, const int* rp, const int* ci, int nsys
 //   rows             A*x and the ISAI rows: fma over the row, from 0.0; ISAI in
 //                    float when fp32 (input rounded, output widened)
 //   LU solve         in-place factors: input rounded to FT; lower rows ascending,
-//                    s = fma(l_ik, y_k, s) over k ascending from 0, y_i = y_i - s;
-//                    upper rows descending, s = fma(u_ik, z_k, s) over k descending
-//                    from 0, z_i = (y_i - s) * rinv_i, rinv_i = 1.0 / u_ii (FP64,
+//                    a = y_i, a = fma(-l_ik, y_k, a) over k ascending, y_i = a;
+//                    upper rows descending, a = y_i, a = fma(-u_ik, z_k, a) over k
+//                    descending, z_i = a * rinv_i, rinv_i = 1.0 / u_ii (FP64,
 //                    rounded to float for FP32 factors); output widened
 // pv: 0 none, 1 z = aiU (aiL v), 2 z = aiA v, 3 z = U^-1 L^-1 v (in-place LU
 // factors on the factor pattern given as the `l` triangle).  No reference
 // counterpart.
 namespace {
 
-// FAST LU solve in FP64: the level-scheduled kernel computes each row from
-// rows finished in earlier levels, so the row-sequential order below gives the
-// same values.
-inline void trsv_lu_fast(int n, const int* rp, const int* ci, const int* diag, const double* lu,
-                         const double* rinv, const double* v, double* y) {
+// FAST LU solve (T = double, or float for FP32 factors with the input already
+// rounded): the level-scheduled kernel computes each row from rows finished in
+// earlier levels, so the row-sequential order below gives the same values.
+template <typename T>
+inline void trsv_lu_fast(int n, const int* rp, const int* ci, const int* diag, const T* lu, const T* rinv, T* y) {
   for (int i = 0; i < n; ++i) {
-    double s = 0.0;
-    for (int k = rp[i]; k < diag[i]; ++k) s = std::fma(lu[k], y[ci[k]], s);
-    y[i] = v[i] - s;
+    T a = y[i];
+    for (int k = rp[i]; k < diag[i]; ++k) a = std::fma(-lu[k], y[ci[k]], a);
+    y[i] = a;
   }
   for (int i = n - 1; i >= 0; --i) {
-    double s = 0.0;
-    for (int k = rp[i + 1] - 1; k > diag[i]; --k) s = std::fma(lu[k], y[ci[k]], s);
-    y[i] = (y[i] - s) * rinv[i];
+    T a = y[i];
+    for (int k = rp[i + 1] - 1; k > diag[i]; --k) a = std::fma(-lu[k], y[ci[k]], a);
+    y[i] = a * rinv[i];
   }
 }
 
@@ -763,10 +763,14 @@ ORC_API int orc_bicgstab_fast(int n, int nnz, const int* rp, const int* ci, int 
       if (pv == 0) {
         sph = in;
       } else if (pv == 3) {
-        if (fp32)
-          trsv_lu_f32(n, l_rp, l_ci, ldiag.data(), Lf, rinvf.data(), in.data(), inf.data(), sph.data());
-        else
-          trsv_lu_fast(n, l_rp, l_ci, ldiag.data(), Ld, rinvd.data(), in.data(), sph.data());
+        if (fp32) {
+          for (int i = 0; i < n; ++i) inf[i] = (float)in[i];
+          trsv_lu_fast<float>(n, l_rp, l_ci, ldiag.data(), Lf, rinvf.data(), inf.data());
+          for (int i = 0; i < n; ++i) sph[i] = (double)inf[i];
+        } else {
+          sph = in;
+          trsv_lu_fast<double>(n, l_rp, l_ci, ldiag.data(), Ld, rinvd.data(), sph.data());
+        }
       } else if (fp32) {
         for (int i = 0; i < n; ++i) inf[i] = (float)in[i];
         if (pv == 1) {

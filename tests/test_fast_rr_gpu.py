@@ -208,3 +208,20 @@ def test_rr_lu_edge_cases(cuda):
         assert g["status"][1] == 2 and g["status"][2] == 3 and g["status"][4] == -3
         if max_iter == 2:
             assert g["status"][0] == -1
+
+
+@pytest.mark.parametrize("fam,precond,kw", [("3d7_7x7x7", bilu.PRECOND_PARILU0_ISAI, dict(parilu_sweeps=5)),
+                                            ("cd2d_12x12", bilu.PRECOND_ILU0, dict(ilu_approach=1)),
+                                            ("3d7_5x5x5", bilu.PRECOND_GENERAL_ISAI, dict(isai_power=2))],
+                         ids=["parilu_isai", "merged_ilu0", "general_isai"])
+@pytest.mark.parametrize("staging", [0, 8, 9, 14])
+@pytest.mark.parametrize("fp32", [False, True])
+def test_rr_operand_layouts_bitwise(cuda, fam, precond, kw, staging, fp32):
+    """Shared-memory staging and the SELL-32 copies of A and aiU change where the SpMVs read their operands,
+    never the arithmetic: every layout equals the oracle bit for bit."""
+    rp, ci, v, b = H.workload(fam, NSYS)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, reduction=bilu.REDUCE_FAST, smem_staging=staging,
+                    factor_precision=bilu.FP32 if fp32 else bilu.FP64, **kw, **TOL)
+    o = _oracle_fast(rp, ci, v, b, precond, g["info"]["threads"], fp32, approach=kw.get("ilu_approach", 1),
+                     sweeps=kw.get("parilu_sweeps", 5), power=kw.get("isai_power", 2), **TOL)
+    _check(g, o, f"{fam} precond {precond} staging {staging} fp32={fp32}")
