@@ -195,6 +195,11 @@ __host__ __device__ inline SmemLayout layout_for(int n, int annz, int fnnz, int 
   return L;
 }
 
+// Triangular-solve program of one triangle (DevPattern::tp_*) from its level
+// schedule (n <= 1024): header pairs {off, w} per level and the slot words.
+void build_trsv_program(const int* rp, const int* ci, const int* diag, const std::vector<int>& lptr,
+                        const std::vector<int>& lrows, bool upper, std::vector<int>& hdr, std::vector<int>& prog);
+
 // Shared-memory carve-up of the register-resident FAST solver (k_solve_rr.cu):
 // reduction slots, the SpMV input (FP64), the preconditioner input and
 // intermediate (FT), for LU preconditioners the in-place factors (FP64 while
@@ -204,6 +209,29 @@ struct RRLayout {
   int red = -1, ph = -1, in = -1, mid = -1, F = -1, rinv = -1, A = -1, ail = -1, aiu = -1, total = 0;
 };
 
+// The mandatory part of an RRLayout (no optional staging), the same on host
+// and device: pv 0 none, 1 two-triangle ISAI, 2 general ISAI, 3 ILU factors
+// (inkernel: the FP64 factorisation slot of the merged form).
+__host__ __device__ inline RRLayout rr_layout_base(int n, int nnz, int pv, bool fp32, bool inkernel) {
+  RRLayout L;
+  int off = 0;
+  const int fts = fp32 ? 4 : 8;
+  auto take = [&](int& dst, long long bytes) {
+    dst = off;
+    off = (int)((off + bytes + 15) & ~15LL);
+  };
+  take(L.red, 4 * 64 * 8);
+  take(L.ph, (long long)n * 8);
+  if (pv == 1 || pv == 2 || (pv == 3 && fp32)) take(L.in, (long long)n * fts);
+  if (pv == 1) take(L.mid, (long long)n * fts);
+  if (pv == 3) {
+    take(L.F, (long long)nnz * (inkernel ? 8 : fts));
+    take(L.rinv, (long long)n * fts);
+  }
+  L.total = off;
+  return L;
+}
+
 // One system of an uneven batch (own size and pattern); offsets in ints into
 // the plan's metadata buffer, value / vector offsets into the concatenated
 // batch arrays.
@@ -212,6 +240,7 @@ struct SysDesc {
   int nlev_lo, nlev_up;
   long long val_off, vec_off;
   int o_rp, o_ci, o_diag, o_llp, o_llr, o_lup, o_lur, o_dp, o_dep;
+  int o_tlh, o_tl, o_tuh, o_tu;  // triangular-solve programs (n <= 1024; else 0)
 };
 
 struct UnevenArgs {
@@ -225,6 +254,10 @@ struct UnevenArgs {
 };
 
 // kernel launch wrappers (k_solve.cu / k_factor.cu)
+// register-resident solver over one uneven-batch bucket: CTA b solves system
+// order[b] with nt threads, R rows per thread (pv 0 none, 3 merged ILU(0))
+const void* rr_uneven_kernel(int pv, int fp32, int R);
+cudaError_t launch_uneven_rr(const UnevenArgs& u, int nt, int R, int pv, int fp32, cudaStream_t st);
 void* uneven_kernel(int fp32, int reduce_fast, int maxl);
 cudaError_t launch_uneven(const UnevenArgs& u, int threads, int grid, int fp32, int reduce_fast, int maxl,
                           cudaStream_t st);

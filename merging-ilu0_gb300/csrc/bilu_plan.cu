@@ -96,6 +96,35 @@ void pattern_deps(int n, const int* rp, const int* ci, const int* diag, std::vec
     }
 }
 
+void build_trsv_program(const int* rp, const int* ci, const int* diag, const std::vector<int>& lptr,
+                        const std::vector<int>& lrows, bool upper, std::vector<int>& hdr, std::vector<int>& prog) {
+  hdr.clear();
+  prog.clear();
+  for (int l = 0; l + 1 < (int)lptr.size(); ++l) {
+    const int w = lptr[l + 1] - lptr[l];
+    int maxc = 0;
+    for (int q = lptr[l]; q < lptr[l + 1]; ++q) {
+      const int i = lrows[q];
+      maxc = std::max(maxc, upper ? rp[i + 1] - 1 - diag[i] : diag[i] - rp[i]);
+    }
+    const int rows_e = std::max(maxc, kTrsvPrefetch);
+    const int off = (int)prog.size();
+    hdr.push_back(off);
+    hdr.push_back(w);
+    prog.resize(off + (size_t)w * (1 + rows_e), 0);
+    for (int s = 0; s < w; ++s) {
+      const int i = lrows[lptr[l] + s];
+      int j = 0;
+      if (upper) {
+        for (int k = rp[i + 1] - 1; k > diag[i]; --k, ++j) prog[off + w + (size_t)j * w + s] = k << 10 | ci[k];
+      } else {
+        for (int k = rp[i]; k < diag[i]; ++k, ++j) prog[off + w + (size_t)j * w + s] = k << 10 | ci[k];
+      }
+      prog[off + s] = i | j << 10;
+    }
+  }
+}
+
 }  // namespace bilu
 
 using namespace bilu;
@@ -136,34 +165,10 @@ void build_trsv_programs(bilu_plan& P) {
   P.tp_up_hdr.clear();
   P.tp_up.clear();
   if (P.n > 1024) return;
-  auto build = [&](const std::vector<int>& lptr, const std::vector<int>& lrows, bool upper, std::vector<int>& hdr,
-                   std::vector<int>& prog) {
-    for (int l = 0; l + 1 < (int)lptr.size(); ++l) {
-      const int w = lptr[l + 1] - lptr[l];
-      int maxc = 0;
-      for (int q = lptr[l]; q < lptr[l + 1]; ++q) {
-        const int i = lrows[q];
-        maxc = std::max(maxc, upper ? P.rp[i + 1] - 1 - P.diag[i] : P.diag[i] - P.rp[i]);
-      }
-      const int rows_e = std::max(maxc, bilu::kTrsvPrefetch);
-      const int off = (int)prog.size();
-      hdr.push_back(off);
-      hdr.push_back(w);
-      prog.resize(off + (size_t)w * (1 + rows_e), 0);
-      for (int s = 0; s < w; ++s) {
-        const int i = lrows[lptr[l] + s];
-        int j = 0;
-        if (upper) {
-          for (int k = P.rp[i + 1] - 1; k > P.diag[i]; --k, ++j) prog[off + w + (size_t)j * w + s] = k << 10 | P.ci[k];
-        } else {
-          for (int k = P.rp[i]; k < P.diag[i]; ++k, ++j) prog[off + w + (size_t)j * w + s] = k << 10 | P.ci[k];
-        }
-        prog[off + s] = i | j << 10;
-      }
-    }
-  };
-  build(P.lev_lo_ptr, P.lev_lo_rows, false, P.tp_lo_hdr, P.tp_lo);
-  build(P.lev_up_ptr, P.lev_up_rows, true, P.tp_up_hdr, P.tp_up);
+  bilu::build_trsv_program(P.rp.data(), P.ci.data(), P.diag.data(), P.lev_lo_ptr, P.lev_lo_rows, false, P.tp_lo_hdr,
+                           P.tp_lo);
+  bilu::build_trsv_program(P.rp.data(), P.ci.data(), P.diag.data(), P.lev_up_ptr, P.lev_up_rows, true, P.tp_up_hdr,
+                           P.tp_up);
 }
 
 // SELL-32 layout of a pattern with n <= 1024 rows (DevPattern::sa_* / su_*).
@@ -355,22 +360,14 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   const int pv = pk == PK_NONE ? 0 : (lu ? 3 : (P.general_isai ? 2 : 1));
   const bool fp32 = is_fp32(o);
   const int fts = fp32 ? 4 : 8;
-  RRLayout L;
-  int off = 0;
+  if (pv == 3 && P.tp_lo.empty()) return false;
+  // the merged form factorises in FP64 in the factor slot before rounding to FT
+  RRLayout L = rr_layout_base(n, P.nnz, pv, fp32, pk == PK_ILU_INKERNEL);
+  int off = L.total;
   auto take = [&](int& dst, long long bytes) {
     dst = off;
     off = (int)((off + bytes + 15) & ~15LL);
   };
-  take(L.red, 4 * 64 * 8);
-  take(L.ph, (long long)n * 8);
-  if (pv == 1 || pv == 2 || (pv == 3 && fp32)) take(L.in, (long long)n * fts);
-  if (pv == 1) take(L.mid, (long long)n * fts);
-  if (pv == 3) {
-    if (P.tp_lo.empty()) return false;
-    // the merged form factorises in FP64 in this slot before rounding to FT
-    take(L.F, (long long)P.nnz * (pk == PK_ILU_INKERNEL ? 8 : fts));
-    take(L.rinv, (long long)n * fts);
-  }
   int dev = 0, per_sm = 0, reserved = 0, optin = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);

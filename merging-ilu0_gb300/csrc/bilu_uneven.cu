@@ -4,13 +4,15 @@
 //
 // The reference needs one shared pattern per batch (ReadWriteData.cpp:398-433);
 // here every system carries its own pattern.  The host analyses each pattern
-// once (diagonal pointers, level schedules, dependency pairs; OpenMP over
-// systems), sorts the systems into size buckets, and each bucket runs as one
-// persistent kernel whose CTAs take systems from an atomic work queue,
-// longest first.  The per-bucket CTA size and grid come from an autotuner
-// that times the candidates on the caller's batch.  All bucket launches (and
-// the zeroing of their queue heads) are captured once into a CUDA graph whose
-// branches run concurrently; a solve is one graph launch.
+// once (diagonal pointers, level schedules, dependency pairs, triangular-solve
+// programs; OpenMP over systems) and sorts the systems into size buckets,
+// longest first.  In the reference operation order each bucket runs as one
+// persistent kernel whose CTAs take systems from an atomic work queue; in FAST
+// order, buckets of systems with n <= 1024 run the register-resident solver,
+// one CTA per system.  The per-bucket CTA size (and persistent grid) come from
+// an autotuner that times the candidates on the caller's batch.  All bucket
+// launches (and the zeroing of the queue heads) are captured once into a CUDA
+// graph whose branches run concurrently; a solve is one graph launch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,6 +37,8 @@ struct Bucket {
   int grid = 0;              // persistent CTAs
   float tuned_ms = -1.0f;
   int maxn = 0;
+  bool rr = false;           // register-resident solver, one CTA per system (FAST order, n <= 1024)
+  int R = 0;                 // its rows per thread
 };
 
 }  // namespace
@@ -98,6 +102,27 @@ UnevenArgs make_args(const bilu_uneven_plan* U, const Bucket& b, int bi, const d
   return u;
 }
 
+int rr_pv(const bilu_options& o) { return o.precond == BILU_PRECOND_NONE ? 0 : 3; }
+
+// Sets the register-resident configuration of bucket b for nt threads per
+// system; false when it does not fit (rows per thread, registers, shared memory).
+bool rr_setup(const bilu_uneven_plan* U, Bucket& b, int nt) {
+  const int R = rr_rows_per_thread(b.maxn, nt);
+  if (R == 0 || nt % 32 || nt > rr_max_threads(R)) return false;
+  const void* k = rr_uneven_kernel(rr_pv(U->opts), U->opts.factor_precision == BILU_FP32, R);
+  int occ = 0;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, b.smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, nt, b.smem) != cudaSuccess || occ < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  b.rr = true;
+  b.R = R;
+  b.threads = nt;
+  b.grid = (int)b.sys.size();
+  return true;
+}
+
 int occupancy_grid(const bilu_uneven_plan* U, const Bucket& b, int threads) {
   const bool fp32 = U->opts.factor_precision == BILU_FP32;
   const bool fast = U->opts.reduction == BILU_REDUCE_FAST;
@@ -119,8 +144,9 @@ bilu_status launch_bucket(bilu_uneven_plan* U, int bi, const double* vals, const
   const Bucket& b = U->buckets[bi];
   if (b.sys.empty()) return BILU_OK;
   const UnevenArgs u = make_args(U, b, bi, vals, rhs, x, R);
-  cudaError_t e = launch_uneven(u, b.threads, b.grid, U->opts.factor_precision == BILU_FP32,
-                                U->opts.reduction == BILU_REDUCE_FAST, b.maxl, st);
+  cudaError_t e = b.rr ? launch_uneven_rr(u, b.threads, b.R, rr_pv(U->opts), U->opts.factor_precision == BILU_FP32, st)
+                       : launch_uneven(u, b.threads, b.grid, U->opts.factor_precision == BILU_FP32,
+                                       U->opts.reduction == BILU_REDUCE_FAST, b.maxl, st);
   return e == cudaSuccess ? BILU_OK : cuda_fail(e, "uneven launch");
 }
 
@@ -139,7 +165,9 @@ bilu_status capture(bilu_uneven_plan* U, const double* vals, const double* rhs, 
   for (int bi = 0; bi < nb; ++bi) {
     const Bucket& b = U->buckets[bi];
     if (b.sys.empty()) continue;
-    void* k = uneven_kernel(U->opts.factor_precision == BILU_FP32, U->opts.reduction == BILU_REDUCE_FAST, b.maxl);
+    const void* k = b.rr ? rr_uneven_kernel(rr_pv(U->opts), U->opts.factor_precision == BILU_FP32, b.R)
+                         : uneven_kernel(U->opts.factor_precision == BILU_FP32, U->opts.reduction == BILU_REDUCE_FAST,
+                                         b.maxl);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, b.smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
   }
@@ -206,7 +234,7 @@ bilu_status bilu_uneven_plan_create(bilu_uneven_plan** out, int nsys, const int*
   }
   // per-system analysis
   struct Meta {
-    std::vector<int> rp, ci, diag, llp, llr, lup, lur, dp, dep;
+    std::vector<int> rp, ci, diag, llp, llr, lup, lur, dp, dep, tlh, tl, tuh, tu;
     int maxw = 0, maxl = 0;
     int err = 0;
   };
@@ -239,6 +267,10 @@ bilu_status bilu_uneven_plan_create(bilu_uneven_plan** out, int nsys, const int*
       pattern_levels(n, rp, ci, m.diag.data(), m.llp, m.llr, wl, m.lup, m.lur, wu);
       m.maxw = std::max(wl, wu);
       pattern_deps(n, rp, ci, m.diag.data(), m.dp, m.dep);
+      if (n <= 1024 && o.reduction == BILU_REDUCE_FAST) {
+        build_trsv_program(rp, ci, m.diag.data(), m.llp, m.llr, false, m.tlh, m.tl);
+        build_trsv_program(rp, ci, m.diag.data(), m.lup, m.lur, true, m.tuh, m.tu);
+      }
     }
   }
   for (int s = 0; s < nsys; ++s) {
@@ -286,6 +318,10 @@ bilu_status bilu_uneven_plan_create(bilu_uneven_plan** out, int nsys, const int*
     d.o_lur = put(m.lur);
     d.o_dp = put(m.dp);
     d.o_dep = put(m.dep);
+    d.o_tlh = put(m.tlh);
+    d.o_tl = put(m.tl);
+    d.o_tuh = put(m.tuh);
+    d.o_tu = put(m.tu);
     m = Meta();  // release the per-system copies
   }
   if (meta.size() > (size_t)0x7fffffff) {
@@ -319,6 +355,16 @@ bilu_status bilu_uneven_plan_create(bilu_uneven_plan** out, int nsys, const int*
       b.smem = std::max(b.smem, L.total);
       b.maxl = std::max(b.maxl, U->desc[s].maxl);
       b.maxn = std::max(b.maxn, h_sys_n[s]);
+    }
+    // FAST order: the register-resident solver's layout for every system of the bucket
+    if (fast && !b.sys.empty() && b.maxn <= 1024) {
+      int rsm = 0;
+      for (int s : b.sys)
+        rsm = std::max(rsm, rr_layout_base(h_sys_n[s], h_sys_nnz[s], rr_pv(o), fp32, true).total);
+      if (rsm <= budget) {
+        b.rr = true;
+        b.smem = rsm;
+      }
     }
     if (b.smem > budget) {
       const int need = b.smem;
@@ -354,8 +400,21 @@ bilu_status bilu_uneven_plan_create(bilu_uneven_plan** out, int nsys, const int*
     bilu_uneven_plan_destroy(U);
     return st;
   }
-  for (auto& b : U->buckets)
-    if (!b.sys.empty()) b.grid = occupancy_grid(U, b, b.threads);
+  for (auto& b : U->buckets) {
+    if (b.sys.empty()) continue;
+    if (b.rr) {
+      // default: the fewest warps that give the largest system 8 rows per thread
+      if (!rr_setup(U, b, round32((b.maxn + 7) / 8))) {
+        b.rr = false;  // back to the shared-memory kernel and its layout
+        b.smem = 0;
+        for (int s : b.sys)
+          b.smem = std::max(b.smem, layout_for(h_sys_n[s], h_sys_nnz[s], h_sys_nnz[s], prec_kind_uneven(o), fp32,
+                                               fast, 0, 0, budget).total);
+        b.threads = std::min(1024, round32(std::max(b.maxn, 64)));
+      }
+    }
+    if (!b.rr) b.grid = occupancy_grid(U, b, b.threads);
+  }
   *out = U;
   return BILU_OK;
 }
@@ -387,14 +446,23 @@ bilu_status bilu_uneven_autotune(bilu_uneven_plan* U, const double* d_values, co
   for (int bi = 0; bi < (int)U->buckets.size() && !res; ++bi) {
     Bucket& b = U->buckets[bi];
     if (b.sys.empty()) continue;
-    int best_t = b.threads, best_g = b.grid;
+    int best_t = b.threads, best_g = b.grid, best_R = b.R;
     float best = 1e30f;
-    for (int t : cands) {
-      const int g = occupancy_grid(U, b, t);
-      if (g <= 0) continue;
+    const int rr_base = round32((b.maxn + 7) / 8);
+    const int rr_cands[] = {rr_base, 2 * rr_base, 4 * rr_base, 0, 0};
+    for (int ci = 0; ci < 5; ++ci) {
+      const int t = b.rr ? rr_cands[ci] : cands[ci];
+      if (t <= 0) continue;
       Bucket trial = b;
-      trial.threads = t;
-      trial.grid = g;
+      if (b.rr) {
+        if (!rr_setup(U, trial, t)) continue;
+      } else {
+        const int g = occupancy_grid(U, b, t);
+        if (g <= 0) continue;
+        trial.threads = t;
+        trial.grid = g;
+      }
+      const int g = trial.grid, tR = trial.R;
       std::swap(U->buckets[bi], trial);
       float ms_min = 1e30f;
       for (int rep = 0; rep < 2 && !res; ++rep) {
@@ -413,10 +481,12 @@ bilu_status bilu_uneven_autotune(bilu_uneven_plan* U, const double* d_values, co
         best = ms_min;
         best_t = t;
         best_g = g;
+        best_R = tR;
       }
     }
     b.threads = best_t;
     b.grid = best_g;
+    b.R = best_R;
     b.tuned_ms = best;
   }
   cudaEventDestroy(e0);

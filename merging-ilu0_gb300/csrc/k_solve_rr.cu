@@ -214,18 +214,16 @@ __device__ __forceinline__ void lu_apply(const DevPattern& P, const FT* __restri
 // 3 in-place ILU factors (a.prec: PK_ILU_INKERNEL factorises A here,
 // PK_LU_GLOBAL reads a.F).
 // FT: type of the ISAI values / factors and of the preconditioner arithmetic.
+// Solves system `sys` (result slot) with the CTA: P its pattern, L its
+// shared-memory carve-up, Ag / bg / xg its values, right-hand side and
+// solution.  Block-wide.
 template <int R, int PV, typename FT>
-__global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 : 128)), R == 8 ? 3 : 1)
-    k_bicgstab_rr(const SolveArgs a, const RRLayout L) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int sys = blockIdx.x;
-  if (sys >= a.nsys) return;
-  const DevPattern& P = a.pat;
+__device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P, const RRLayout& L,
+                                         unsigned char* smem, const int sys, const double* Ag, const double* bg,
+                                         double* xg) {
   const int n = P.n, nt = blockDim.x, tid = threadIdx.x, nw = nt >> 5;
   const int* __restrict__ arp = P.a_rp;
   const int* __restrict__ aci = P.a_ci;
-  const double* Ag = a.A + (size_t)sys * P.a_nnz;
-  const double* bg = a.b + (size_t)sys * n;
 
   double* red = reinterpret_cast<double*>(smem + L.red);  // 4 slots of 2 * 32
   double* sph = reinterpret_cast<double*>(smem + L.ph);
@@ -482,7 +480,6 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
 #undef BILU_RR_INPUT
 
   // ---- write back
-  double* xg = a.x + (size_t)sys * n;
 #pragma unroll
   for (int k = 0; k < R; ++k) {
     const int i = tid + k * nt;
@@ -525,6 +522,52 @@ __global__ void __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 
   }
 }
 
+#define BILU_RR_BOUNDS __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 : 128)), R == 8 ? 3 : 1)
+
+// one CTA per system of a batch sharing one pattern
+template <int R, int PV, typename FT>
+__global__ void BILU_RR_BOUNDS k_bicgstab_rr(const SolveArgs a, const RRLayout L) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sys = blockIdx.x;
+  if (sys >= a.nsys) return;
+  const DevPattern& P = a.pat;
+  rr_solve<R, PV, FT>(a, P, L, smem, sys, a.A + (size_t)sys * P.a_nnz, a.b + (size_t)sys * P.n,
+                      a.x + (size_t)sys * P.n);
+}
+
+// one CTA per system of an uneven-batch bucket (own size and pattern each):
+// CTA b solves system order[b] (longest first), merged ILU(0) (PV 3) or none
+// (PV 0), no optional staging
+template <int R, int PV, typename FT>
+__global__ void BILU_RR_BOUNDS k_bicgstab_rr_uneven(const UnevenArgs u) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  if ((int)blockIdx.x >= u.count) return;
+  const int sys = __ldg(u.order + blockIdx.x);
+  const SysDesc d = u.desc[sys];
+  DevPattern P;
+  P.n = d.n;
+  P.nnz = P.a_nnz = d.nnz;
+  P.a_maxl = d.maxl;
+  P.rp = P.a_rp = u.meta + d.o_rp;
+  P.ci = P.a_ci = u.meta + d.o_ci;
+  P.diag = u.meta + d.o_diag;
+  P.nlev_lo = d.nlev_lo;
+  P.nlev_up = d.nlev_up;
+  P.maxw_lo = P.maxw_up = d.maxw;
+  P.lev_lo_ptr = u.meta + d.o_llp;
+  P.lev_lo_rows = u.meta + d.o_llr;
+  P.lev_up_ptr = u.meta + d.o_lup;
+  P.lev_up_rows = u.meta + d.o_lur;
+  P.dep_ptr = u.meta + d.o_dp;
+  P.dep = reinterpret_cast<const int2*>(u.meta + d.o_dep);
+  P.tp_lo_hdr = reinterpret_cast<const int2*>(u.meta + d.o_tlh);
+  P.tp_lo = u.meta + d.o_tl;
+  P.tp_up_hdr = reinterpret_cast<const int2*>(u.meta + d.o_tuh);
+  P.tp_up = u.meta + d.o_tu;
+  const RRLayout L = rr_layout_base(d.n, d.nnz, PV, sizeof(FT) == 4, true);
+  rr_solve<R, PV, FT>(u.base, P, L, smem, sys, u.base.A + d.val_off, u.base.b + d.vec_off, u.base.x + d.vec_off);
+}
+
 template <int R, int PV, typename FT>
 cudaError_t launch_rr_t(const SolveArgs& a, const RRLayout& L, int nt, cudaStream_t st) {
   auto k = k_bicgstab_rr<R, PV, FT>;
@@ -554,7 +597,30 @@ cudaError_t launch_rr_pv(const SolveArgs& a, const RRLayout& L, int nt, int R, c
   }
 }
 
+template <int PV, typename FT>
+const void* rr_uneven_kernel_pv(int R) {
+  switch (R) {
+    case 1: return (const void*)k_bicgstab_rr_uneven<1, PV, FT>;
+    case 2: return (const void*)k_bicgstab_rr_uneven<2, PV, FT>;
+    case 4: return (const void*)k_bicgstab_rr_uneven<4, PV, FT>;
+    default: return (const void*)k_bicgstab_rr_uneven<8, PV, FT>;
+  }
+}
+
 }  // namespace
+
+const void* rr_uneven_kernel(int pv, int fp32, int R) {
+  if (pv == 0) return rr_uneven_kernel_pv<0, double>(R);
+  return fp32 ? rr_uneven_kernel_pv<3, float>(R) : rr_uneven_kernel_pv<3, double>(R);
+}
+
+// Dynamic shared memory = u.smem_budget (the bucket's largest layout); the
+// caller has set the kernel's shared-memory attribute outside any capture.
+cudaError_t launch_uneven_rr(const UnevenArgs& u, int nt, int R, int pv, int fp32, cudaStream_t st) {
+  if (u.count == 0) return cudaSuccess;
+  void* args[] = {const_cast<UnevenArgs*>(&u)};
+  return cudaLaunchKernel(rr_uneven_kernel(pv, fp32, R), dim3(u.count), dim3(nt), args, (size_t)u.smem_budget, st);
+}
 
 int rr_rows_per_thread(int n, int nt) {
   for (int R : {1, 2, 4, 8})

@@ -1,6 +1,8 @@
 """Uneven batches (own size and pattern per system): one graph-launched solve
-of persistent, size-bucketed kernels, checked per system against the oracle
-bit for bit in the reference operation order."""
+of size-bucketed kernels, checked per system against the oracle bit for bit,
+in the reference operation order (persistent shared-memory kernels) and in
+FAST order (the register-resident solver, one CTA per system, its bucket's
+threads per system)."""
 import numpy as np
 import pytest
 
@@ -69,15 +71,59 @@ def test_uneven_autotune_keeps_bits_and_graph_replays(cuda):
             assert i["threads"] in (64, 128, 256, 512, 1024) and i["grid"] > 0 and i["tuned_ms"] > 0
 
 
-def test_uneven_fast_mode(cuda):
-    sn, sz, rp, ci, v, b = bilu.gen_uneven(48, seed=9, nmin=64, nmax=1024)
-    with bilu.UnevenPlan(sn, sz, rp, ci, tol_mode=bilu.TOL_REL, tol=1e-10, reduction=bilu.REDUCE_FAST) as plan:
-        g, _ = _run(cuda, plan, v, b, len(sn))
+def _oracle_uneven_fast(sn, sz, rp, ci, v, b, info, fp32, precond=bilu.PRECOND_ILU0, **tol):
+    """orc_bicgstab_fast per system with its bucket's threads per system (merged ILU(0), approach 1)."""
+    import oracle as O
+    out = {f: [] for f in ("x", "iters", "conv", "res", "true_res", "status")}
+    for s, (r, c, vv, bb) in enumerate(H.uneven_split(sn, sz, rp, ci, v, b)):
+        n = int(sn[s])
+        nt = next(i["threads"] for i in info if i["n_lo"] < n <= i["n_hi"])
+        if precond == bilu.PRECOND_NONE:
+            o = O.bicgstab_fast(r, c, vv[None, :], bb[None, :], nt, pv=0, **tol)
+        else:
+            lu = O.ilu0(r, c, vv[None, :], 1)
+            o = O.bicgstab_fast(r, c, vv[None, :], bb[None, :], nt, pv=3, ail=(r, c, lu), fp32=fp32, **tol)
+        for f in out:
+            out[f].append(o[f][0])
+    return {"x": np.concatenate(out["x"]), "iters": np.array(out["iters"], np.float32),
+            "conv": np.array(out["conv"], np.int32), "res": np.array(out["res"]),
+            "true_res": np.array(out["true_res"]), "status": np.array(out["status"], np.int32)}
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_uneven_fast_bitwise(cuda, fp32):
+    """FAST order: every bucket with n <= 1024 runs the register-resident solver; bit for bit against the
+    oracle's restatement of its order, before and after autotuning (which changes threads per system)."""
+    import torch
+    sn, sz, rp, ci, v, b = bilu.gen_uneven(48, seed=9, nmin=16, nmax=1024)
+    tol = dict(tol_mode=bilu.TOL_REL, tol=1e-10)
+    with bilu.UnevenPlan(sn, sz, rp, ci, reduction=bilu.REDUCE_FAST,
+                         factor_precision=bilu.FP32 if fp32 else bilu.FP64, **tol) as plan:
+        g, bufs = _run(cuda, plan, v, b, len(sn))
+        info = plan.info()
+        assert sum(1 for i in info if i["systems"]) >= 3
+        _cmp(g, _oracle_uneven_fast(sn, sz, rp, ci, v, b, info, fp32, **tol), f"uneven FAST fp32={fp32}")
+        V, B, X = bufs[:3]
+        plan.autotune(V, B, torch.empty_like(X))
+        torch.cuda.synchronize()
+        g2, _ = _run(cuda, plan, v, b, len(sn))
+        info2 = plan.info()
+        _cmp(g2, _oracle_uneven_fast(sn, sz, rp, ci, v, b, info2, fp32, **tol), f"uneven FAST autotuned fp32={fp32}")
     parts = H.uneven_split(sn, sz, rp, ci, v, b)
     bn = np.array([np.linalg.norm(p[3]) for p in parts])
     assert np.all(g["conv"] == 1)
     assert np.all(g["res"] < 1e-10 * bn)
     assert np.all(g["true_res"] < 1e-8 * bn)
+
+
+def test_uneven_fast_unpreconditioned_bitwise(cuda):
+    sn, sz, rp, ci, v, b = bilu.gen_uneven(24, seed=4, nmin=16, nmax=400)
+    tol = dict(tol_mode=bilu.TOL_ABS, tol=1e-11, max_iter=60)
+    with bilu.UnevenPlan(sn, sz, rp, ci, precond=bilu.PRECOND_NONE, reduction=bilu.REDUCE_FAST, **tol) as plan:
+        g, _ = _run(cuda, plan, v, b, len(sn))
+        info = plan.info()
+    _cmp(g, _oracle_uneven_fast(sn, sz, rp, ci, v, b, info, False, precond=bilu.PRECOND_NONE, **tol),
+         "uneven FAST, no preconditioner")
 
 
 def test_uneven_rejects_missing_diagonal(cuda):
