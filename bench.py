@@ -35,9 +35,9 @@ METRIC = "systems solved/sec at rel. residual 1e-10: chosen vs plain form, % HBM
 
 # workloads: (kind, gx, gy, gz, nsys, options)
 HEADLINE = dict(name="parilu5_isai_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096, autotune=True,
-                desc="ParILU(0) 5 sweeps + ISAI(L,U on |T|^2) BiCGSTAB, ISAI stored and applied in FP32 (A*x, inner "
-                     "products, recurrences, ParILU in FP64), 4096 FP64 systems, 3D 7-point 10x10x10 (n=1000, "
-                     "nnz=6400), Peclet skew U(0,0.5), rel. tol 1e-10, max 500 iterations",
+                desc="ParILU(0) 5 sweeps + ISAI(L,U on |T|^2) BiCGSTAB, ISAI computed, stored and applied in FP32 "
+                     "(A*x, inner products, recurrences, ParILU in FP64), 4096 FP64 systems, 3D 7-point 10x10x10 "
+                     "(n=1000, nnz=6400), Peclet skew U(0,0.5), rel. tol 1e-10, max 500 iterations",
                 opts=dict(precond=4, parilu_sweeps=5, isai_power=2, tol_mode=1, tol=1e-10, max_iter=500,
                           reduction=1, factor_precision=1), fwd_sample=32)
 SECONDARY = [
@@ -342,8 +342,9 @@ def measure_uneven(dev, stream, nsys=8192, steps=3, warmup=2):
             "buckets": [{k: i[k] for k in ("n_hi", "systems", "threads", "grid", "smem_bytes", "tuned_ms")}
                         for i in info if i["systems"]],
             "workload": "uneven batch: 8192 FP64 systems, n log-uniform in [64,1024], 5-12 random off-diagonals per "
-                        "row, diag 1.2x abs row sum with random sign, merged ILU(0), FAST order, rel 1e-10, autotuned "
-                        "size buckets, one CUDA-graph launch per step"}
+                        "row, diag 1.2x abs row sum with random sign, merged ILU(0), FAST order (register-resident "
+                        "solver, one CTA per system), rel 1e-10, autotuned threads per system per size bucket, one "
+                        "CUDA-graph launch per step"}
 
 
 def measure_learned(dev, stream, ntrain=65536, neval=16384, train_steps=1500, batch=65536, steps=3):

@@ -269,6 +269,65 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
   for (int k = threadIdx.x; k < P.aiu_nnz; k += blockDim.x) aiu[(size_t)sys * P.aiu_nnz + k] = (FT)M[k];
 }
 
+// FAST ISAI stored in FP32 (BILU_REDUCE_FAST with BILU_FP32), computed in
+// FP32: the factors are rounded to float once into shared memory, every
+// product is an fmaf in the order of k_isai's program, and the aiU entries are
+// multiplied by the float reciprocal of the rounded diagonal (__frcp_rn, the
+// value of 1.0f / u).  The result is what the solver applies (FP32 values,
+// FP32 arithmetic); the FP64 pipe only rounds the factors.  No reference
+// counterpart (the library's definition; orc_isai_values_ex mode 2).
+__global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, const double* __restrict__ LUg,
+                                                  float* __restrict__ ail, float* __restrict__ aiu) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sys = blockIdx.x;
+  if (sys >= nsys) return;
+  const int n = P.n, nnz = P.nnz;
+  float* LU = reinterpret_cast<float*>(smem);
+  float* M = LU + nnz;                                                  // max(ail_nnz, aiu_nnz)
+  float* rinv = M + (P.ail_nnz > P.aiu_nnz ? P.ail_nnz : P.aiu_nnz);  // n
+  for (int k = threadIdx.x; k < nnz; k += blockDim.x) LU[k] = (float)__ldg(LUg + (size_t)sys * nnz + k);
+  __syncthreads();
+  // ---- aiL (unit diagonal)
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int beg = __ldg(P.ail_rp + i), sz = __ldg(P.ail_rp + i + 1) - beg;
+    float* m = M + beg;
+    m[sz - 1] = 1.0f;
+    int q = __ldg(P.ail_prog_ptr + i);
+    for (int blk = 0; blk < sz - 1; ++blk) {
+      const int2 h = __ldg(P.ail_prog + q++);
+      float acc = 0.0f;
+      for (int u = 0; u < h.y; ++u) {
+        const int2 e = __ldg(P.ail_prog + q++);
+        acc = fmaf(-m[e.x], LU[e.y], acc);
+      }
+      m[h.x] = acc;
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < P.ail_nnz; k += blockDim.x) ail[(size_t)sys * P.ail_nnz + k] = M[k];
+  __syncthreads();
+  // ---- aiU
+  for (int i = threadIdx.x; i < n; i += blockDim.x) rinv[i] = __frcp_rn(LU[__ldg(P.diag + i)]);
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int beg = __ldg(P.aiu_rp + i), sz = __ldg(P.aiu_rp + i + 1) - beg;
+    float* m = M + beg;
+    m[0] = rinv[i];
+    int q = __ldg(P.aiu_prog_ptr + i);
+    for (int blk = 1; blk < sz; ++blk) {
+      const int2 h = __ldg(P.aiu_prog + q++);
+      float acc = 0.0f;
+      for (int u = 0; u < h.y; ++u) {
+        const int2 e = __ldg(P.aiu_prog + q++);
+        acc = fmaf(-m[e.x], LU[e.y], acc);
+      }
+      m[h.x] = acc * rinv[__ldg(P.aiu_ci + beg + h.x)];
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < P.aiu_nnz; k += blockDim.x) aiu[(size_t)sys * P.aiu_nnz + k] = M[k];
+}
+
 // ---------------------------------------------------------------- general ISAI
 // ISAI of A itself (solve_general_dense, isai_gpu.cu:392-554), one thread per
 // ISAI row and system.  Lane t of the reference holds row t of A(J,J)^T; here
@@ -435,9 +494,11 @@ cudaError_t launch_parilu0(const DevPattern& p, int nsys, const double* A, const
 cudaError_t launch_isai(const DevPattern& p, int nsys, const double* lu, void* ail, void* aiu, int fp32, int threads,
                         cudaStream_t st, int fast) {
   if (nsys == 0) return cudaSuccess;
-  const int smem = (p.nnz + (p.ail_nnz > p.aiu_nnz ? p.ail_nnz : p.aiu_nnz) + (fast ? p.n : 0)) * 8;
-  void* k = fp32 ? (fast ? (void*)k_isai<float, true> : (void*)k_isai<float, false>)
-                 : (fast ? (void*)k_isai<double, true> : (void*)k_isai<double, false>);
+  const bool f32 = fp32 && fast && !p.l_diag;  // FAST FP32 ISAI: computed in FP32 (k_isai_f32)
+  const int smem = (p.nnz + (p.ail_nnz > p.aiu_nnz ? p.ail_nnz : p.aiu_nnz) + (fast ? p.n : 0)) * (f32 ? 4 : 8);
+  void* k = f32 ? (void*)k_isai_f32
+                : fp32 ? (fast ? (void*)k_isai<float, true> : (void*)k_isai<float, false>)
+                       : (fast ? (void*)k_isai<double, true> : (void*)k_isai<double, false>);
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<DevPattern*>(&p), &nsys, &lu, &ail, &aiu};

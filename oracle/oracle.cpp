@@ -436,6 +436,45 @@ ORC_API int orc_isai_values_ex(int n, const int* t_rp, const int* t_ci, int t_nn
                                int tri, const int* ai_rp, const int* ai_ci, int ai_nnz, double* ai_vals, int fast) {
   for (int i = 0; i < n; ++i)
     if (ai_rp[i + 1] - ai_rp[i] > 32) return -1;
+  if (fast == 2 && tri != 2) {
+    // the library's FAST ISAI stored in FP32 (k_isai_f32): T rounded to float,
+    // float fmas in the same order, aiU scaled by 1.0f / u (float); L's unit
+    // diagonal is exact.  Values returned widened to double.
+#pragma omp parallel for schedule(static)
+    for (int s = 0; s < nsys; ++s) {
+      const double* T = t_vals + (size_t)s * t_nnz;
+      double* M = ai_vals + (size_t)s * ai_nnz;
+      float loc[32][32];
+      for (int i = 0; i < n; ++i) {
+        const int beg = ai_rp[i], sz = ai_rp[i + 1] - ai_rp[i];
+        const int* J = ai_ci + beg;
+        for (int t = 0; t < sz; ++t)
+          for (int c = 0; c < sz; ++c) {
+            float v = 0.0f;
+            for (int k = t_rp[J[c]]; k < t_rp[J[c] + 1]; ++k)
+              if (t_ci[k] == J[t]) v = (float)T[k];
+            loc[t][c] = v;
+          }
+        float sol[32];
+        if (tri == 0) {
+          for (int t = 0; t < sz; ++t) sol[t] = (t == sz - 1) ? 1.0f : 0.0f;
+          for (int col = sz - 1; col >= 0; --col) {
+            const float bot = sol[col];  // unit diagonal
+            for (int t = 0; t < col; ++t) sol[t] = std::fma(-bot, loc[t][col], sol[t]);
+          }
+        } else {
+          for (int t = 0; t < sz; ++t) sol[t] = (t == 0) ? 1.0f : 0.0f;
+          for (int col = 0; col < sz; ++col) {
+            sol[col] = sol[col] * (1.0f / loc[col][col]);
+            const float top = sol[col];
+            for (int t = col + 1; t < sz; ++t) sol[t] = std::fma(-top, loc[t][col], sol[t]);
+          }
+        }
+        for (int t = 0; t < sz; ++t) M[beg + t] = (double)sol[t];
+      }
+    }
+    return 0;
+  }
 #pragma omp parallel for schedule(static)
   for (int s = 0; s < nsys; ++s) {
     const double* T = t_vals + (size_t)s * t_nnz;

@@ -148,12 +148,13 @@ def isai_pattern(rp, ci, power, vals0=None):
 
 
 def isai_values(trp, tci, tvals, tri, arp, aci, fast=False):
-    """fast: the reciprocal-multiply upper-triangle ISAI of BILU_REDUCE_FAST."""
+    """fast: True (1) = the reciprocal-multiply upper-triangle ISAI of BILU_REDUCE_FAST; 2 = the FAST ISAI
+    stored in FP32, computed in FP32 (values returned widened to float64)."""
     trp, tci, arp, aci = _ia(trp), _ia(tci), _ia(arp), _ia(aci)
     tvals = np.ascontiguousarray(tvals, np.float64)
     out = np.zeros((tvals.shape[0], len(aci)))
     r = lib().orc_isai_values_ex(len(trp) - 1, _i(trp), _i(tci), tvals.shape[1], tvals.shape[0], _d(tvals),
-                                 int(tri), _i(arp), _i(aci), len(aci), _d(out), int(bool(fast)))
+                                 int(tri), _i(arp), _i(aci), len(aci), _d(out), int(fast))
     if r != 0:
         raise ValueError("ISAI row longer than 32")
     return out

@@ -40,8 +40,8 @@ def _oracle_fast(rp, ci, v, b, precond, nt, fp32, approach=3, sweeps=5, power=2,
     Lv, Uv = O.split_values(nrp, nci, lu)
     arp, aci = O.isai_pattern(lrp, lci, power)
     brp, bci = O.isai_pattern(urp, uci, power)
-    ail = O.isai_values(lrp, lci, Lv, 0, arp, aci)
-    aiu = O.isai_values(urp, uci, Uv, 1, brp, bci, fast=True)
+    ail = O.isai_values(lrp, lci, Lv, 0, arp, aci, fast=2 if fp32 else False)
+    aiu = O.isai_values(urp, uci, Uv, 1, brp, bci, fast=2 if fp32 else True)
     return O.bicgstab_fast(rp, ci, v, b, nt, pv=1, ail=(arp, aci, ail), aiu=(brp, bci, aiu), fp32=fp32, **tol)
 
 
