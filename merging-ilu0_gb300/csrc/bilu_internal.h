@@ -15,6 +15,8 @@ namespace bilu {
 // entries per row of a triangular-solve program that the register-resident
 // solver loads one level ahead (the rest it loads when it needs them)
 constexpr int kTrsvPrefetch = 4;
+// op words per row of an ILU(0) program loaded one level ahead
+constexpr int kIluPrefetch = 16;
 
 // learned warm start: 9 features -> 64 -> 64 -> 1
 constexpr int kMlpFeatures = 9;
@@ -88,6 +90,15 @@ struct DevPattern {
   const int* tp_lo = nullptr;
   const int2* tp_up_hdr = nullptr;
   const int* tp_up = nullptr;
+  // ILU(0) program of the register-resident solver's merged form (n <= 1024),
+  // per lower level: header {off, w, len, 0}; slot s word j at prog[off + j*w + s]:
+  // word 0 = number of op words that follow; ops per entry k of the row in
+  // column order (upper entries without pairs, exact no-ops, left out):
+  // k | pairs << 20 | lower << 30, then for a lower entry the diagonal position
+  // of its column, then the pairs (l position, u position) in summation order.
+  // Every level has at least kIluPrefetch + 1 words per slot.
+  const int4* ilu_hdr = nullptr;
+  const int* ilu_prog = nullptr;
   // SELL-32 copies for the register-resident solver's SpMVs, of A (sa_*) and of
   // aiU (su_*): slice s holds rows 32s .. 32s+31, entry j of row 32s+l at
   // off[s] + 32j + l, so a warp's 32 rows read one contiguous line per entry;
@@ -199,6 +210,10 @@ __host__ __device__ inline SmemLayout layout_for(int n, int annz, int fnnz, int 
 // schedule (n <= 1024): header pairs {off, w} per level and the slot words.
 void build_trsv_program(const int* rp, const int* ci, const int* diag, const std::vector<int>& lptr,
                         const std::vector<int>& lrows, bool upper, std::vector<int>& hdr, std::vector<int>& prog);
+// ILU(0) program (DevPattern::ilu_*) of the factor pattern for one approach (1..4).
+void build_ilu_program(const int* rp, const int* ci, const int* diag, const std::vector<int>& lptr,
+                       const std::vector<int>& lrows, const std::vector<int>& dep_ptr, const std::vector<int>& dep,
+                       int approach, std::vector<int>& hdr, std::vector<int>& prog);
 
 // Shared-memory carve-up of the register-resident FAST solver (k_solve_rr.cu):
 // reduction slots, the SpMV input (FP64), the preconditioner input and
@@ -241,6 +256,7 @@ struct SysDesc {
   long long val_off, vec_off;
   int o_rp, o_ci, o_diag, o_llp, o_llr, o_lup, o_lur, o_dp, o_dep;
   int o_tlh, o_tl, o_tuh, o_tu;  // triangular-solve programs (n <= 1024; else 0)
+  int o_ih, o_ip;                // ILU(0) program (n <= 1024; else 0)
 };
 
 struct UnevenArgs {
@@ -320,6 +336,7 @@ struct bilu_plan {
   std::vector<int> l_rp, l_ci, l_src, u_rp, u_ci, u_src;
   std::vector<int> row_lev, tpos, mlp_ent;
   std::vector<int> tp_lo_hdr, tp_lo, tp_up_hdr, tp_up;  // triangular-solve programs (DevPattern::tp_*)
+  std::vector<int> ilu_hdr, ilu_prog;                    // ILU(0) program (DevPattern::ilu_*)
   std::vector<int> sa_off, sa_ci, sa_src, su_off, su_ci, su_src;  // SELL-32 layouts (DevPattern::sa_*, su_*)
   std::vector<int> pl_ent;  // ParILU entry classes (see DevPattern::pl_ent)
   int pl_ndep = 0, pl_nlow = 0;

@@ -125,6 +125,43 @@ void build_trsv_program(const int* rp, const int* ci, const int* diag, const std
   }
 }
 
+void build_ilu_program(const int* rp, const int* ci, const int* diag, const std::vector<int>& lptr,
+                       const std::vector<int>& lrows, const std::vector<int>& dep_ptr, const std::vector<int>& dep,
+                       int approach, std::vector<int>& hdr, std::vector<int>& prog) {
+  hdr.clear();
+  prog.clear();
+  std::vector<std::vector<int>> slot;
+  for (int l = 0; l + 1 < (int)lptr.size(); ++l) {
+    const int w = lptr[l + 1] - lptr[l];
+    slot.assign(w, {});
+    int len = kIluPrefetch + 1;
+    for (int s = 0; s < w; ++s) {
+      const int i = lrows[lptr[l] + s];
+      std::vector<int>& ops = slot[s];
+      ops.push_back(0);
+      for (int k = rp[i]; k < rp[i + 1]; ++k) {
+        const int j = ci[k], pb = dep_ptr[k], pe = dep_ptr[k + 1], np = pe - pb;
+        const bool lower = j < i;
+        if (!lower && np == 0) continue;  // a = a: an exact no-op in every approach
+        ops.push_back(k | np << 20 | (lower ? 1 : 0) << 30);
+        if (lower) ops.push_back(diag[j]);
+        for (int q = 0; q < np; ++q) {
+          const int qq = approach == 2 ? pe - 1 - q : pb + q;  // approach 2 sums the pairs descending
+          ops.push_back(dep[2 * qq]);
+          ops.push_back(dep[2 * qq + 1]);
+        }
+      }
+      ops[0] = (int)ops.size() - 1;
+      len = std::max(len, (int)ops.size());
+    }
+    const int off = (int)prog.size();
+    hdr.insert(hdr.end(), {off, w, len, 0});
+    prog.resize(off + (size_t)w * len, 0);
+    for (int s = 0; s < w; ++s)
+      for (int j = 0; j < (int)slot[s].size(); ++j) prog[off + (size_t)j * w + s] = slot[s][j];
+  }
+}
+
 }  // namespace bilu
 
 using namespace bilu;
@@ -196,7 +233,15 @@ void build_sell(int n, const std::vector<int>& rp, const std::vector<int>& ci, s
   }
 }
 
-void build_deps(bilu_plan& P) { bilu::pattern_deps(P.n, P.rp.data(), P.ci.data(), P.diag.data(), P.dep_ptr, P.dep); }
+void build_deps(bilu_plan& P) {
+  bilu::pattern_deps(P.n, P.rp.data(), P.ci.data(), P.diag.data(), P.dep_ptr, P.dep);
+  P.ilu_hdr.clear();
+  P.ilu_prog.clear();
+  // the merged form's in-kernel ILU(0) in the register-resident solver (n <= 1024, 20-bit positions)
+  if (P.n <= 1024 && P.nnz < (1 << 20) && P.opts.precond == BILU_PRECOND_ILU0)
+    bilu::build_ilu_program(P.rp.data(), P.ci.data(), P.diag.data(), P.lev_lo_ptr, P.lev_lo_rows, P.dep_ptr, P.dep,
+                            P.opts.ilu_approach, P.ilu_hdr, P.ilu_prog);
+}
 
 // structural pattern of T^power, T given by (trp, tci)
 void pattern_power(int n, const std::vector<int>& trp, const std::vector<int>& tci, int power, std::vector<int>& orp,
@@ -431,6 +476,7 @@ bilu_status upload(bilu_plan& P) {
   const size_t o_plent = put(P.pl_ent);
   const size_t o_tlh = put(P.tp_lo_hdr), o_tl = put(P.tp_lo), o_tuh = put(P.tp_up_hdr), o_tu = put(P.tp_up);
   const size_t o_sao = put(P.sa_off), o_sac = put(P.sa_ci), o_sas = put(P.sa_src);
+  const size_t o_ih = put(P.ilu_hdr), o_ip = put(P.ilu_prog);
   const size_t o_suo = put(P.su_off), o_suc = put(P.su_ci), o_sus = put(P.su_src);
   size_t o_alrp = 0, o_alci = 0, o_aurp = 0, o_auci = 0, o_alpp = 0, o_alp = 0, o_aupp = 0, o_aup = 0;
   size_t o_gmp = 0, o_gm = 0, o_gp = 0;
@@ -486,6 +532,10 @@ bilu_status upload(bilu_plan& P) {
   d.n_mlp = (int)P.mlp_ent.size();
   d.mlp_ent = b + o_ment;
   d.pl_ent = b + o_plent;
+  if (!P.ilu_prog.empty()) {
+    d.ilu_hdr = reinterpret_cast<const int4*>(b + o_ih);
+    d.ilu_prog = b + o_ip;
+  }
   if (!P.sa_off.empty()) {
     d.sa_nnz = P.sa_off.back();
     d.sa_off = b + o_sao;

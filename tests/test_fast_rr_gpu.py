@@ -139,6 +139,8 @@ def test_rr_autotuned_plan_bitwise(cuda):
 LU_CASES = [
     ("2d5_16x16", bilu.PRECOND_ILU0, dict(ilu_approach=1)),
     ("3d7_7x7x7", bilu.PRECOND_ILU0, dict(ilu_approach=4)),
+    ("cd2d_12x12", bilu.PRECOND_ILU0, dict(ilu_approach=2)),
+    ("3d7_5x5x5", bilu.PRECOND_ILU0, dict(ilu_approach=3)),
     ("cd2d_12x12", bilu.PRECOND_ILU0_SPLIT, dict(ilu_approach=3)),
     ("3d7_5x5x5", bilu.PRECOND_ILU0_SPLIT, dict(ilu_approach=2)),
     ("3d7_7x7x7", bilu.PRECOND_PARILU0, dict(parilu_sweeps=4)),
