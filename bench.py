@@ -444,12 +444,21 @@ def main():
     ap.add_argument("--nsys", type=int, default=0, help="override the headline batch size (profiling runs)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the plan's default solver configuration (profiling runs: fixed launch sequence)")
+    ap.add_argument("--workload", default="",
+                    help="with --kernel-only: measure this secondary workload (by name) instead of the headline "
+                         "(profiling runs)")
     args = ap.parse_args()
+    if args.workload:
+        found = [w for w in SECONDARY if w["name"] == args.workload]
+        if not found or not args.kernel_only:
+            ap.error("--workload needs --kernel-only and one of: " + ", ".join(w["name"] for w in SECONDARY))
+        HEADLINE.clear()
+        HEADLINE.update(found[0])
     if args.no_autotune:
         HEADLINE["autotune"] = False
     if args.nsys > 0:
+        HEADLINE["desc"] = HEADLINE["desc"].replace(f"{HEADLINE['nsys']} FP64", f"{args.nsys} FP64")
         HEADLINE["nsys"] = args.nsys
-        HEADLINE["desc"] = HEADLINE["desc"].replace("4096 FP64", f"{args.nsys} FP64")
     if args.impl == "reference":
         run_reference_arm(args)
         return
