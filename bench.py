@@ -10,9 +10,9 @@ the library's C ABI.  `value` is measured with the inputs resident in HBM;
 `e2e` adds the pinned host->device copy of the step's values and right-hand
 sides and the device->host copy of the solutions and per-system results.
 
-Under torchrun (N > 1) every rank solves its own full batch on its own GPU
-(weak scaling, no collective on the data path); the step time is the maximum
-over ranks.  --impl reference times the CPU restatement of the reference's
+Under torchrun (N > 1) rank r solves systems r*B .. (r+1)*B-1 of one seeded
+global batch on its own GPU (shard.py; weak scaling, no collective on the data
+path); the step time is the maximum over ranks.  --impl reference times the CPU restatement of the reference's
 solver (the reference has no CPU path of its own) on the host cores.
 """
 import argparse
@@ -187,11 +187,12 @@ def run_reference_arm(args):
     print(json.dumps(line))
 
 
-def measure(wl, steps, warmup, dev, stream, sampler=None, e2e=False, timed_hook=None):
+def measure(wl, steps, warmup, dev, stream, sampler=None, e2e=False, timed_hook=None, first=0):
+    """first: index of this rank's first system in the seeded global batch (its slab)."""
     import torch
     import bilu
     kind, (gx, gy, gz), nsys = wl["kind"], wl["grid"], wl["nsys"]
-    rp, ci, v, b = bilu.gen_stencil(kind, gx, gy, gz, nsys, SEED)
+    rp, ci, v, b = bilu.gen_stencil(kind, gx, gy, gz, nsys, SEED, first=first)
     n, nnz = len(rp) - 1, len(ci)
     plan = bilu.Plan(rp, ci, **wl["opts"])
     plan.enable_timing(True)
@@ -482,8 +483,10 @@ def main():
         torch.cuda.synchronize()
 
     sampler = ClockSampler(local)
+    import shard
+    first, _ = shard.slab(HEADLINE["nsys"] * world, rank, world)  # B systems per rank (weak scaling)
     res = measure(HEADLINE, args.steps, max(args.warmup, 3), dev, stream, sampler=sampler,
-                  e2e=not args.kernel_only, timed_hook=barrier)
+                  e2e=not args.kernel_only, timed_hook=barrier, first=first)
     if args.kernel_only:
         if rank == 0:
             print(json.dumps({k: res[k] for k in ("name", "nsys", "ms_total", "steps", "systems_per_s", "setup_ms",
@@ -491,9 +494,7 @@ def main():
         return
     ms = res["ms_total"]
     if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = shard.max_over_ranks(ms, device=dev)
         e = torch.tensor([res["e2e"]["value"]], device=dev)
         dist.all_reduce(e, op=dist.ReduceOp.SUM)
         res["e2e"]["value"] = float(e.item())
@@ -576,7 +577,8 @@ def main():
                    else "fp64", "threads_per_system": info["threads"], "solver_kernel": info["solver_kernel"],
                    "smem_bytes_per_system": info["smem_bytes"],
                    "l2": "inputs larger than L2: A values %.0f MB per step" % (nsys * nnz * 8 / 1e6),
-                   "parallelism": f"weak: {world} independent batch(es), one per GPU"},
+                   "parallelism": f"weak: {world} slab(s) of {nsys} systems of one seeded batch, one per GPU, "
+                                  f"no collective on the data path"},
         "clocks": res["clocks"],
         "e2e": res["e2e"],
         "gpu_launches": 3 * args.steps,

@@ -379,6 +379,13 @@ bilu_status bilu_gen_stencil(int kind, int gx, int gy, int gz, int nsys, uint64_
                              int* n, int* nnz, int* h_row_ptrs, int* h_col_idxs,
                              double* h_values, double* h_b);
 
+/* Systems first .. first+nsys-1 of the same seeded stream (system s of
+ * bilu_gen_stencil is system s here): each rank of a multi-GPU run generates
+ * its own slab of one global batch.  No reference counterpart. */
+bilu_status bilu_gen_stencil_range(int kind, int gx, int gy, int gz, long long first, int nsys, uint64_t seed,
+                                   int* n, int* nnz, int* h_row_ptrs, int* h_col_idxs,
+                                   double* h_values, double* h_b);
+
 /* Uneven batch (per-system sizes and patterns): n_s = floor(exp(U(ln nmin, ln nmax))),
  * per row k ~ U{kmin..kmax} distinct off-diagonal columns plus the diagonal
  * (sorted), off-diagonals ~ N(0,1), a_ii = 1.2 * sum_j |a_ij| * sign, sign ~ U{+-1};

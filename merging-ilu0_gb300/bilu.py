@@ -30,7 +30,8 @@ EXPORTED = [
     "bilu_default_options", "bilu_plan_create", "bilu_plan_destroy", "bilu_plan_get_info",
     "bilu_plan_get_pattern", "bilu_expand_values", "bilu_solve", "bilu_solve_warm", "bilu_ilu0",
     "bilu_parilu0", "bilu_split_lu", "bilu_isai", "bilu_true_residual", "bilu_last_error",
-    "bilu_version", "bilu_device_count", "bilu_gen_stencil", "bilu_gen_uneven", "bilu_plan_enable_timing",
+    "bilu_version", "bilu_device_count", "bilu_gen_stencil", "bilu_gen_stencil_range", "bilu_gen_uneven",
+    "bilu_plan_enable_timing",
     "bilu_plan_last_timing", "bilu_plan_autotune", "bilu_solve_noalloc", "bilu_uneven_plan_create", "bilu_uneven_plan_destroy",
     "bilu_uneven_autotune", "bilu_uneven_solve", "bilu_uneven_get_info", "bilu_forward_error",
     "bilu_mlp_create", "bilu_mlp_destroy", "bilu_mlp_param_count", "bilu_mlp_get_params", "bilu_mlp_set_params",
@@ -121,6 +122,8 @@ def lib():
         L.bilu_plan_last_timing.argtypes = [vp, C.POINTER(Timing)]
         L.bilu_gen_uneven.argtypes = [i, C.c_uint64, i, i, i, i, ip, ip, ip, ip, C.POINTER(d), C.POINTER(d)]
         L.bilu_gen_stencil.argtypes = [i, i, i, i, i, C.c_uint64, ip, ip, ip, ip, C.POINTER(d), C.POINTER(d)]
+        L.bilu_gen_stencil_range.argtypes = [i, i, i, i, C.c_longlong, i, C.c_uint64, ip, ip, ip, ip, C.POINTER(d),
+                                             C.POINTER(d)]
         _lib = L
     return _lib
 
@@ -167,16 +170,17 @@ def version():
 
 
 # ---------------------------------------------------------------- generators
-def gen_stencil(kind, gx, gy, gz, nsys, seed=20261203):
-    """Seeded batch of a stencil workload: returns (row_ptrs, col_idxs, values[nsys, nnz], b[nsys, n])."""
+def gen_stencil(kind, gx, gy, gz, nsys, seed=20261203, first=0):
+    """Seeded batch of a stencil workload: returns (row_ptrs, col_idxs, values[nsys, nnz], b[nsys, n]).
+    first > 0: systems first .. first+nsys-1 of the same seeded stream (a rank's slab of a global batch)."""
     n, nnz = C.c_int(), C.c_int()
     _check(lib().bilu_gen_stencil(kind, gx, gy, gz, 0, seed, C.byref(n), C.byref(nnz), None, None, None, None))
     rp = np.zeros(n.value + 1, np.int32)
     ci = np.zeros(nnz.value, np.int32)
     vals = np.zeros((nsys, nnz.value), np.float64)
     b = np.zeros((nsys, n.value), np.float64)
-    _check(lib().bilu_gen_stencil(kind, gx, gy, gz, nsys, seed, C.byref(n), C.byref(nnz), _iptr(rp), _iptr(ci),
-                                  _dptr(vals), _dptr(b)))
+    _check(lib().bilu_gen_stencil_range(kind, gx, gy, gz, int(first), nsys, seed, C.byref(n), C.byref(nnz),
+                                        _iptr(rp), _iptr(ci), _dptr(vals), _dptr(b)))
     return rp, ci, vals, b
 
 

@@ -62,10 +62,12 @@ static void stencil_pattern(int gx, int gy, int gz, std::vector<int>& rp, std::v
 
 using namespace bilu;
 
-extern "C" bilu_status bilu_gen_stencil(int kind, int gx, int gy, int gz, int nsys, uint64_t seed,
-                                        int* n_out, int* nnz_out, int* h_row_ptrs, int* h_col_idxs,
-                                        double* h_values, double* h_b) {
-  if (gx <= 0 || gy <= 0 || gz <= 0 || nsys < 0) return set_error(BILU_ERR_INVALID, "bilu_gen_stencil: bad sizes");
+// systems first .. first+nsys-1 of the seeded stream (system s draws from Rng(seed, s))
+static bilu_status gen_stencil(int kind, int gx, int gy, int gz, long long first, int nsys, uint64_t seed,
+                               int* n_out, int* nnz_out, int* h_row_ptrs, int* h_col_idxs, double* h_values,
+                               double* h_b) {
+  if (gx <= 0 || gy <= 0 || gz <= 0 || nsys < 0 || first < 0)
+    return set_error(BILU_ERR_INVALID, "bilu_gen_stencil: bad sizes");
   if (!(kind == 1 || kind == 2 || kind == 4 || kind == 5))
     return set_error(BILU_ERR_INVALID, "bilu_gen_stencil: kind must be 1, 2, 4 or 5");
   std::vector<int> rp, ci;
@@ -80,7 +82,7 @@ extern "C" bilu_status bilu_gen_stencil(int kind, int gx, int gy, int gz, int ns
 
 #pragma omp parallel for schedule(static)
   for (int s = 0; s < nsys; ++s) {
-    Rng rng(seed, (uint64_t)s);
+    Rng rng(seed, (uint64_t)(first + s));
     double peclet = 0.0;
     if (kind == 2) peclet = 0.5 * rng.u01();
     if (kind == 4) peclet = 2.0 * rng.u01();
@@ -125,6 +127,18 @@ extern "C" bilu_status bilu_gen_stencil(int kind, int gx, int gy, int gz, int ns
     }
   }
   return BILU_OK;
+}
+
+extern "C" bilu_status bilu_gen_stencil(int kind, int gx, int gy, int gz, int nsys, uint64_t seed, int* n_out,
+                                        int* nnz_out, int* h_row_ptrs, int* h_col_idxs, double* h_values,
+                                        double* h_b) {
+  return gen_stencil(kind, gx, gy, gz, 0, nsys, seed, n_out, nnz_out, h_row_ptrs, h_col_idxs, h_values, h_b);
+}
+
+extern "C" bilu_status bilu_gen_stencil_range(int kind, int gx, int gy, int gz, long long first, int nsys,
+                                              uint64_t seed, int* n_out, int* nnz_out, int* h_row_ptrs,
+                                              int* h_col_idxs, double* h_values, double* h_b) {
+  return gen_stencil(kind, gx, gy, gz, first, nsys, seed, n_out, nnz_out, h_row_ptrs, h_col_idxs, h_values, h_b);
 }
 
 // Uneven batch: per-system sizes n_s = floor(exp(U(ln nmin, ln nmax))), per row
