@@ -99,6 +99,13 @@ struct DevPattern {
   // Every level has at least kIluPrefetch + 1 words per slot.
   const int4* ilu_hdr = nullptr;
   const int* ilu_prog = nullptr;
+  // 16-bit copies of the column indices read by the register-resident solver's
+  // SpMVs (n <= 65535): half the L1 footprint of the int32 arrays
+  const unsigned short* a_ci16 = nullptr;
+  const unsigned short* ail_ci16 = nullptr;
+  const unsigned short* aiu_ci16 = nullptr;
+  const unsigned short* sa_ci16 = nullptr;
+  const unsigned short* su_ci16 = nullptr;
   // SELL-32 copies for the register-resident solver's SpMVs, of A (sa_*) and of
   // aiU (su_*): slice s holds rows 32s .. 32s+31, entry j of row 32s+l at
   // off[s] + 32j + l, so a warp's 32 rows read one contiguous line per entry;

@@ -477,6 +477,23 @@ bilu_status upload(bilu_plan& P) {
   const size_t o_tlh = put(P.tp_lo_hdr), o_tl = put(P.tp_lo), o_tuh = put(P.tp_up_hdr), o_tu = put(P.tp_up);
   const size_t o_sao = put(P.sa_off), o_sac = put(P.sa_ci), o_sas = put(P.sa_src);
   const size_t o_ih = put(P.ilu_hdr), o_ip = put(P.ilu_prog);
+  // 16-bit column indices, two per int
+  auto put16 = [&](const std::vector<int>& v) {
+    std::vector<int> packed((v.size() + 1) / 2, 0);
+    for (size_t q = 0; q < v.size(); ++q) {
+      const unsigned int u = (unsigned int)v[q] & 0xFFFFu;
+      packed[q / 2] |= (int)(u << (16 * (q % 2)));
+    }
+    return put(packed);
+  };
+  const bool ci16 = P.n <= 65535;
+  const size_t o_a16 = ci16 ? put16(P.in_ci) : 0, o_sa16 = ci16 ? put16(P.sa_ci) : 0;
+  size_t o_l16 = 0, o_u16 = 0, o_su16 = 0;
+  if (ci16 && P.has_isai) {
+    o_l16 = put16(P.ail_ci);
+    o_u16 = put16(P.aiu_ci);
+    o_su16 = put16(P.su_ci);
+  }
   const size_t o_suo = put(P.su_off), o_suc = put(P.su_ci), o_sus = put(P.su_src);
   size_t o_alrp = 0, o_alci = 0, o_aurp = 0, o_auci = 0, o_alpp = 0, o_alp = 0, o_aupp = 0, o_aup = 0;
   size_t o_gmp = 0, o_gm = 0, o_gp = 0;
@@ -532,6 +549,15 @@ bilu_status upload(bilu_plan& P) {
   d.n_mlp = (int)P.mlp_ent.size();
   d.mlp_ent = b + o_ment;
   d.pl_ent = b + o_plent;
+  if (ci16) {
+    d.a_ci16 = reinterpret_cast<const unsigned short*>(b + o_a16);
+    if (!P.sa_ci.empty()) d.sa_ci16 = reinterpret_cast<const unsigned short*>(b + o_sa16);
+    if (P.has_isai) {
+      d.ail_ci16 = reinterpret_cast<const unsigned short*>(b + o_l16);
+      d.aiu_ci16 = reinterpret_cast<const unsigned short*>(b + o_u16);
+      if (!P.su_ci.empty()) d.su_ci16 = reinterpret_cast<const unsigned short*>(b + o_su16);
+    }
+  }
   if (!P.ilu_prog.empty()) {
     d.ilu_hdr = reinterpret_cast<const int4*>(b + o_ih);
     d.ilu_prog = b + o_ip;

@@ -87,8 +87,8 @@ __device__ __forceinline__ double fma_t(double a, double b, double c) { return f
 // step, so the thread has R independent FMA chains in flight (64-cycle FP64
 // latency) instead of one; each row still sums its entries in ascending order
 // from 0.
-template <int R, typename VT, typename XT>
-__device__ __forceinline__ void rows_acc(const VT* __restrict__ val, const int* __restrict__ ci,
+template <int R, typename VT, typename XT, typename IT>
+__device__ __forceinline__ void rows_acc(const VT* __restrict__ val, const IT* __restrict__ ci,
                                          const int* __restrict__ rp, int tid, int nt, int n,
                                          const XT* __restrict__ xv, XT (&out)[R]) {
   int beg[R], len[R];
@@ -201,8 +201,8 @@ __device__ void ilu_program_rows(const DevPattern& P, double* LU, int approach, 
 // same FMAs in the same order; entry j of the warp's 32 rows (tid + k*nt for
 // one k: 32 consecutive rows, one slice) is one contiguous line of values and
 // of column indices.
-template <int R, typename VT, typename XT>
-__device__ __forceinline__ void rows_acc_sell(const VT* __restrict__ val, const int* __restrict__ sci,
+template <int R, typename VT, typename XT, typename IT>
+__device__ __forceinline__ void rows_acc_sell(const VT* __restrict__ val, const IT* __restrict__ sci,
                                               const int* __restrict__ soff, const int* __restrict__ rp, int tid,
                                               int nt, int n, const XT* __restrict__ xv, XT (&out)[R]) {
   int pos[R], len[R];
@@ -303,16 +303,29 @@ __device__ __forceinline__ void lu_apply(const DevPattern& P, const FT* __restri
 // 3 in-place ILU factors (a.prec: PK_ILU_INKERNEL factorises A here,
 // PK_LU_GLOBAL reads a.F).
 // FT: type of the ISAI values / factors and of the preconditioner arithmetic.
+// column indices for the SpMVs: the plan's 16-bit copies (C16) or the int32 arrays
+template <bool C16>
+__device__ __forceinline__ auto pick_ci(const unsigned short* c16, const int* c32) {
+  if constexpr (C16)
+    return c16;
+  else
+    return c32;
+}
+
 // Solves system `sys` (result slot) with the CTA: P its pattern, L its
 // shared-memory carve-up, Ag / bg / xg its values, right-hand side and
 // solution.  Block-wide.
-template <int R, int PV, typename FT>
+template <int R, int PV, typename FT, bool C16>
 __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P, const RRLayout& L,
                                          unsigned char* smem, const int sys, const double* Ag, const double* bg,
                                          double* xg) {
   const int n = P.n, nt = blockDim.x, tid = threadIdx.x, nw = nt >> 5;
   const int* __restrict__ arp = P.a_rp;
-  const int* __restrict__ aci = P.a_ci;
+  const auto* __restrict__ aci = pick_ci<C16>(P.a_ci16, P.a_ci);
+  const auto* __restrict__ lci = pick_ci<C16>(P.ail_ci16, P.ail_ci);
+  const auto* __restrict__ uci = pick_ci<C16>(P.aiu_ci16, P.aiu_ci);
+  const auto* __restrict__ saci = pick_ci<C16>(P.sa_ci16, P.sa_ci);
+  const auto* __restrict__ suci = pick_ci<C16>(P.su_ci16, P.su_ci);
 
   double* red = reinterpret_cast<double*>(smem + L.red);  // 4 slots of 2 * 32
   double* sph = reinterpret_cast<double*>(smem + L.ph);
@@ -440,16 +453,16 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
   do {                                                                                                           \
     if (PV == 1) {                                                                                               \
       FT z_[R];                                                                                                  \
-      rows_acc<R>(AIL, P.ail_ci, P.ail_rp, tid, nt, n, sin, z_);                                                 \
+      rows_acc<R>(AIL, lci, P.ail_rp, tid, nt, n, sin, z_);                                                 \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
         const int i = tid + k * nt;                                                                              \
         if (i < n) smid[i] = z_[k];                                                                              \
       }                                                                                                          \
       __syncthreads();                                                                                           \
       if (AIUsell)                                                                                               \
-        rows_acc_sell<R>(AIUsell, P.su_ci, P.su_off, P.aiu_rp, tid, nt, n, smid, z_);                            \
+        rows_acc_sell<R>(AIUsell, suci, P.su_off, P.aiu_rp, tid, nt, n, smid, z_);                            \
       else                                                                                                       \
-        rows_acc<R>(AIU, P.aiu_ci, P.aiu_rp, tid, nt, n, smid, z_);                                              \
+        rows_acc<R>(AIU, uci, P.aiu_rp, tid, nt, n, smid, z_);                                              \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
         const int i = tid + k * nt;                                                                              \
         if (i < n) sph[i] = (double)z_[k];                                                                       \
@@ -457,7 +470,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
       __syncthreads();                                                                                           \
     } else if (PV == 2) {                                                                                        \
       FT z_[R];                                                                                                  \
-      rows_acc<R>(AIL, P.ail_ci, P.ail_rp, tid, nt, n, sin, z_);                                                 \
+      rows_acc<R>(AIL, lci, P.ail_rp, tid, nt, n, sin, z_);                                                 \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
         const int i = tid + k * nt;                                                                              \
         if (i < n) sph[i] = (double)z_[k];                                                                       \
@@ -495,7 +508,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     BILU_RR_APPLY();  // p_hat in sph
     // v = A p_hat, (r_hat, v)
     if (Asell)
-      rows_acc_sell<R>(Asell, P.sa_ci, P.sa_off, arp, tid, nt, n, sph, v);
+      rows_acc_sell<R>(Asell, saci, P.sa_off, arp, tid, nt, n, sph, v);
     else
       rows_acc<R>(Am, aci, arp, tid, nt, n, sph, v);
     q[0] = 0.0;
@@ -530,7 +543,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     BILU_RR_APPLY();  // s_hat in sph
     // t = A s_hat, (t, s), (t, t)
     if (Asell)
-      rows_acc_sell<R>(Asell, P.sa_ci, P.sa_off, arp, tid, nt, n, sph, t);
+      rows_acc_sell<R>(Asell, saci, P.sa_off, arp, tid, nt, n, sph, t);
     else
       rows_acc<R>(Am, aci, arp, tid, nt, n, sph, t);
     double q2[2] = {0.0, 0.0};
@@ -597,7 +610,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     __syncthreads();
     double ax[R];
     if (Asell)
-      rows_acc_sell<R>(Asell, P.sa_ci, P.sa_off, arp, tid, nt, n, sph, ax);
+      rows_acc_sell<R>(Asell, saci, P.sa_off, arp, tid, nt, n, sph, ax);
     else
       rows_acc<R>(Am, aci, arp, tid, nt, n, sph, ax);
     q[0] = 0.0;
@@ -623,8 +636,8 @@ __global__ void BILU_RR_BOUNDS k_bicgstab_rr(const SolveArgs a, const RRLayout L
   const int sys = blockIdx.x;
   if (sys >= a.nsys) return;
   const DevPattern& P = a.pat;
-  rr_solve<R, PV, FT>(a, P, L, smem, sys, a.A + (size_t)sys * P.a_nnz, a.b + (size_t)sys * P.n,
-                      a.x + (size_t)sys * P.n);
+  rr_solve<R, PV, FT, true>(a, P, L, smem, sys, a.A + (size_t)sys * P.a_nnz, a.b + (size_t)sys * P.n,
+                            a.x + (size_t)sys * P.n);
 }
 
 // one CTA per system of an uneven-batch bucket (own size and pattern each):
@@ -661,7 +674,8 @@ __global__ void BILU_RR_BOUNDS k_bicgstab_rr_uneven(const UnevenArgs u) {
     P.ilu_prog = u.meta + d.o_ip;
   }
   const RRLayout L = rr_layout_base(d.n, d.nnz, PV, sizeof(FT) == 4, true);
-  rr_solve<R, PV, FT>(u.base, P, L, smem, sys, u.base.A + d.val_off, u.base.b + d.vec_off, u.base.x + d.vec_off);
+  rr_solve<R, PV, FT, false>(u.base, P, L, smem, sys, u.base.A + d.val_off, u.base.b + d.vec_off,
+                             u.base.x + d.vec_off);
 }
 
 template <int R, int PV, typename FT>
