@@ -227,3 +227,46 @@ def test_rr_operand_layouts_bitwise(cuda, fam, precond, kw, staging, fp32):
     o = _oracle_fast(rp, ci, v, b, precond, g["info"]["threads"], fp32, approach=kw.get("ilu_approach", 1),
                      sweeps=kw.get("parilu_sweeps", 5), power=kw.get("isai_power", 2), **TOL)
     _check(g, o, f"{fam} precond {precond} staging {staging} fp32={fp32}")
+
+
+def _wide_level_pattern(n=1000, seed=5):
+    """Rows with a diagonal, upper entries (i, i+1) and (i, i+7), and lower entries only in every 97th row:
+    the lower solve (and the ILU(0) schedule) has a first level of ~990 rows, far wider than the CTA, and
+    the upper solve is a chain of n levels."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for i in range(n):
+        cols = {i}
+        if i + 1 < n:
+            cols.add(i + 1)
+        if i + 7 < n:
+            cols.add(i + 7)
+        if i % 97 == 0 and i > 0:
+            cols.add(i - 1)
+            cols.add(i // 2)
+        rows.append(sorted(cols))
+    rp = np.zeros(n + 1, np.int32)
+    rp[1:] = np.cumsum([len(r) for r in rows])
+    ci = np.concatenate([np.array(r, np.int32) for r in rows])
+    return rp, ci, rng
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+@pytest.mark.parametrize("precond", [bilu.PRECOND_ILU0, bilu.PRECOND_ILU0_SPLIT])
+def test_rr_lu_levels_wider_than_cta(cuda, fp32, precond):
+    """Level widths above the CTA size take the solve programs' and the ILU program's second-slot paths."""
+    rp, ci, rng = _wide_level_pattern()
+    nsys, n = 4, len(rp) - 1
+    v = np.empty((nsys, len(ci)))
+    for s in range(nsys):
+        for i in range(n):
+            for k in range(rp[i], rp[i + 1]):
+                v[s, k] = 2.0 + rng.random() if ci[k] == i else -(0.5 + rng.random())
+    b = rng.uniform(-1, 1, (nsys, n))
+    kw = dict(ilu_approach=1) if precond == bilu.PRECOND_ILU0 else dict(ilu_approach=3)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, reduction=bilu.REDUCE_FAST,
+                    factor_precision=bilu.FP32 if fp32 else bilu.FP64, **kw, **TOL)
+    assert g["info"]["threads"] == 128 and g["info"]["levels_lower"] < 10
+    o = _oracle_fast(rp, ci, v, b, precond, 128, fp32, approach=kw["ilu_approach"], **TOL)
+    _check(g, o, f"wide levels precond {precond} fp32={fp32}")
+    assert np.all(g["conv"] == 1)
