@@ -288,8 +288,9 @@ cudaError_t launch_solve(const SolveArgs& a, int threads, int fp32, int reduce_f
 // register-resident FAST solver: pv 0 none, 1 ISAI of L and U, 2 general ISAI
 int rr_rows_per_thread(int n, int nt);  // smallest R in {1, 2, 4, 8} with R * nt >= n, else 0
 int rr_max_threads(int R);
-const void* rr_kernel(int pv, int fp32, int R);
-cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, cudaStream_t st);
+const void* rr_kernel(int pv, int fp32, int R, int ref);  // null: no such variant
+cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, int ref,
+                            cudaStream_t st);
 size_t solve_max_smem();
 cudaError_t launch_expand(const DevPattern& p, int nsys, const double* vin, double* vout, cudaStream_t st);
 cudaError_t launch_ilu0(const DevPattern& p, int nsys, const double* A, double* lu, int approach, int threads,

@@ -396,13 +396,21 @@ void choose_layout(bilu_plan& P) {
 bool rr_configure(bilu_plan& P, int nt, int mask) {
   const bilu_options& o = P.opts;
   const int pk = prec_kind(o.precond);
-  if (o.reduction != BILU_REDUCE_FAST) return false;
+  const bool ref = o.reduction != BILU_REDUCE_FAST;
   const int n = P.n;
   nt = std::max(round_up(nt, 32), 32);
   const int R = rr_rows_per_thread(n, nt);
   if (R == 0 || nt > rr_max_threads(R)) return false;
   const bool lu = (pk == PK_ILU_INKERNEL || pk == PK_LU_GLOBAL);
   const int pv = pk == PK_NONE ? 0 : (lu ? 3 : (P.general_isai ? 2 : 1));
+  // Reference order: one warp per system, whose inner products are the
+  // reference's warp-0 sums; ILU factors or none (the ISAI solvers' serial
+  // inner products stay on the shared-memory kernel), rows of at most 16
+  // entries (row_ref<16>), no SELL-32 copies.
+  if (ref) {
+    if (nt != 32 || (pv != 0 && pv != 3) || P.a_maxl > 16) return false;
+    mask &= 7;
+  }
   const bool fp32 = is_fp32(o);
   const int fts = fp32 ? 4 : 8;
   if (pv == 3 && P.tp_lo.empty()) return false;
@@ -418,7 +426,8 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const void* k = rr_kernel(pv, fp32 ? 1 : 0, R);
+  const void* k = rr_kernel(pv, fp32 ? 1 : 0, R, ref ? 1 : 0);
+  if (!k) return false;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(optin, off)) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, nt, off) != cudaSuccess || occ < 1) {
     cudaGetLastError();
@@ -452,7 +461,8 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
 void choose_rr(bilu_plan& P) {
   const bilu_options& o = P.opts;
   P.rr = false;
-  const int nt = o.threads_per_system > 0 ? o.threads_per_system : round_up((P.n + 7) / 8, 32);
+  int nt = o.threads_per_system > 0 ? o.threads_per_system : round_up((P.n + 7) / 8, 32);
+  if (o.reduction != BILU_REDUCE_FAST && o.threads_per_system <= 0) nt = 32;  // reference order: one warp
   const bool lu = prec_kind(o.precond) == PK_ILU_INKERNEL || prec_kind(o.precond) == PK_LU_GLOBAL;
   rr_configure(P, nt, o.smem_staging >= 0 ? o.smem_staging : (6 | (lu && P.n > 512 ? 8 : 0)));
 }
@@ -1090,7 +1100,8 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
     if (e != cudaSuccess) return cuda_err(e, "SELL copy of A");
     a.A_sell = (const double*)(ws + off_asell);
   }
-  e = P->rr ? launch_solve_rr(a, P->rr_lay, P->rr_threads, P->rr_pv, fp32 ? 1 : 0, st)
+  e = P->rr ? launch_solve_rr(a, P->rr_lay, P->rr_threads, P->rr_pv, fp32 ? 1 : 0,
+                              o.reduction == BILU_REDUCE_FAST ? 0 : 1, st)
             : launch_solve(a, P->threads, fp32 ? 1 : 0, o.reduction == BILU_REDUCE_FAST ? 1 : 0, maxl, st);
   if (e != cudaSuccess) return cuda_err(e, "solver launch");
   if (P->timing) cudaEventRecord(P->ev[2], st);

@@ -37,7 +37,7 @@
 // Reduction order (what orc_bicgstab_fast restates):
 //   thread partial   d = fma(a_i, b_i, d) over its rows in k order, from 0.0
 //   warp             lane values v_l; for off = 16, 8, 4, 2, 1: v_l = v_l + v_(l^off); lane 0's value
-//   block            s = 0.0; s = s + w_j for warps j = 0 .. NT/32-1
+//   block            s = w_0; s = s + w_j for warps j = 1 .. NT/32-1
 //   SpMV row         acc = fma(a_k, x_ci(k), acc), k ascending, from 0.0 (FP64)
 //   ISAI row (FT)    the same in FT; input rounded to FT, output widened to FP64
 //   LU solve (FT)    input rounded to FT; lower row i: a = y_i, a = fma(-l_ik, y_k, a)
@@ -55,6 +55,7 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 
 #include "k_ilu_rows.cuh"
+#include "k_row_ref.cuh"
 
 // K values summed over the CTA; every thread returns the same sums.
 // red: K * 32 doubles of this reduction's own slot.
@@ -73,8 +74,8 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* red, int nw) {
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    double s = 0.0;
-    for (int w = 0; w < nw; ++w) s = s + red[k * 32 + w];
+    double s = red[k * 32];
+    for (int w = 1; w < nw; ++w) s = s + red[k * 32 + w];
     v[k] = s;
   }
 }
@@ -231,13 +232,36 @@ __device__ __forceinline__ void rows_acc_sell(const VT* __restrict__ val, const 
 // Row i starts from y_i and subtracts its products in program order (one FMA
 // each, no separate subtraction); UPPER then scales by rinv_i and also widens
 // z_i into zd for FP32 factors.  Ends with a barrier.
-template <bool UPPER, typename FT>
+// REF: the reference's order instead (PrecondBiCGSTAB_exact_ilu0_app1_merged_gpu.cu:22-108):
+// s = sum of fma(F, y, s) from 0 in program order, then y_i - s, and for UPPER
+// (y_i - s) / u_ii with FP64 factors (rinv then holds u_ii itself) or
+// (y_i - s) * rinv_i with FP32 factors (the library's FP32 definition).
+template <bool UPPER, typename FT, bool REF>
 __device__ __forceinline__ void tri_solve(const int2* __restrict__ hdr, const int* __restrict__ prog, int nlev,
                                           const FT* __restrict__ F, const FT* __restrict__ rinv, FT* y, double* zd,
                                           int tid, int nt) {
   constexpr int PF = kTrsvPrefetch;
   auto row = [&](int rec, const int (&e)[PF], int off, int w, int s) {
     const int i = rec & 1023, cnt = rec >> 10;
+    if (REF) {
+      FT acc = FT(0);
+#pragma unroll
+      for (int j = 0; j < PF; ++j)
+        if (j < cnt) acc = fma_t(F[e[j] >> 10], y[e[j] & 1023], acc);
+      for (int j = PF; j < cnt; ++j) {
+        const int en = __ldg(prog + off + w + j * w + s);
+        acc = fma_t(F[en >> 10], y[en & 1023], acc);
+      }
+      const FT d = y[i] - acc;
+      if (UPPER) {
+        const FT z = sizeof(FT) == 8 ? d / rinv[i] : d * rinv[i];
+        y[i] = z;
+        if (sizeof(FT) == 4) zd[i] = (double)z;
+      } else {
+        y[i] = d;
+      }
+      return;
+    }
     FT acc = y[i];
 #pragma unroll
     for (int j = 0; j < PF; ++j)
@@ -292,11 +316,28 @@ __device__ __forceinline__ void tri_solve(const int2* __restrict__ hdr, const in
 // rounded to FT; for FP64 factors y is the FP64 SpMV input itself, for FP32
 // factors the upper solve widens z into zd).  Ends with a barrier: z is
 // visible to every thread.
-template <typename FT>
+template <typename FT, bool REF>
 __device__ __forceinline__ void lu_apply(const DevPattern& P, const FT* __restrict__ F, const FT* __restrict__ rinv,
                                          FT* y, double* zd, int tid, int nt) {
-  tri_solve<false>(P.tp_lo_hdr, P.tp_lo, P.nlev_lo, F, rinv, y, zd, tid, nt);
-  tri_solve<true>(P.tp_up_hdr, P.tp_up, P.nlev_up, F, rinv, y, zd, tid, nt);
+  tri_solve<false, FT, REF>(P.tp_lo_hdr, P.tp_lo, P.nlev_lo, F, rinv, y, zd, tid, nt);
+  tri_solve<true, FT, REF>(P.tp_up_hdr, P.tp_up, P.nlev_up, F, rinv, y, zd, tid, nt);
+}
+
+// The reference-order SpMV rows (row_ref, the reference's warp-per-row tree
+// for rows of at most 16 entries) for this thread's rows, one row at a time.
+template <int R, typename VT, typename IT>
+__device__ __forceinline__ void rows_acc_ref(const VT* __restrict__ val, const IT* __restrict__ ci,
+                                             const int* __restrict__ rp, int tid, int nt, int n,
+                                             const double* __restrict__ xv, double (&out)[R]) {
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int i = tid + k * nt;
+    out[k] = 0.0;
+    if (i < n) {
+      const int beg = __ldg(rp + i);
+      out[k] = row_ref<16>(val, ci, beg, __ldg(rp + i + 1) - beg, xv);
+    }
+  }
 }
 
 // PV: 0 none, 1 ISAI of L and U (z = aiU (aiL v)), 2 general ISAI (z = aiA v),
@@ -315,7 +356,7 @@ __device__ __forceinline__ auto pick_ci(const unsigned short* c16, const int* c3
 // Solves system `sys` (result slot) with the CTA: P its pattern, L its
 // shared-memory carve-up, Ag / bg / xg its values, right-hand side and
 // solution.  Block-wide.
-template <int R, int PV, typename FT, bool C16>
+template <int R, int PV, typename FT, bool C16, bool REF>
 __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P, const RRLayout& L,
                                          unsigned char* smem, const int sys, const double* Ag, const double* bg,
                                          double* xg) {
@@ -408,7 +449,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     __syncthreads();
     for (int i = tid; i < n; i += nt) {
       const double dgi = (double)Fs[__ldg(P.diag + i)];
-      rinv[i] = (FT)(1.0 / dgi);
+      rinv[i] = (REF && sizeof(FT) == 8) ? (FT)dgi : (FT)(1.0 / dgi);  // REF FP64 divides by u_ii
     }
     // visible to the solves after the first reduction's barrier
   }
@@ -477,7 +518,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
       }                                                                                                          \
       __syncthreads();                                                                                           \
     } else if (PV == 3) {                                                                                        \
-      lu_apply<FT>(P, Fs, rinv, sizeof(FT) == 8 ? reinterpret_cast<FT*>(sph) : sin, sph, tid, nt);              \
+      lu_apply<FT, REF>(P, Fs, rinv, sizeof(FT) == 8 ? reinterpret_cast<FT*>(sph) : sin, sph, tid, nt);         \
     }                                                                                                            \
   } while (0)
 // writes this thread's rows of `vec` as the preconditioner input
@@ -507,7 +548,9 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     __syncthreads();
     BILU_RR_APPLY();  // p_hat in sph
     // v = A p_hat, (r_hat, v)
-    if (Asell)
+    if (REF)
+      rows_acc_ref<R>(Am, aci, arp, tid, nt, n, sph, v);
+    else if (Asell)
       rows_acc_sell<R>(Asell, saci, P.sa_off, arp, tid, nt, n, sph, v);
     else
       rows_acc<R>(Am, aci, arp, tid, nt, n, sph, v);
@@ -542,7 +585,9 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     }
     BILU_RR_APPLY();  // s_hat in sph
     // t = A s_hat, (t, s), (t, t)
-    if (Asell)
+    if (REF)
+      rows_acc_ref<R>(Am, aci, arp, tid, nt, n, sph, t);
+    else if (Asell)
       rows_acc_sell<R>(Asell, saci, P.sa_off, arp, tid, nt, n, sph, t);
     else
       rows_acc<R>(Am, aci, arp, tid, nt, n, sph, t);
@@ -609,6 +654,24 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     }
     __syncthreads();
     double ax[R];
+    if (REF) {
+      // KernelFillTrueResNorms (Bicgstab_common.hpp:294-342): row_ref sums, then one serial
+      // inner product over i = 0 .. n-1 -- the single warp passes each row's residual to every
+      // lane in row order, and every lane runs the same FMA chain
+      rows_acc_ref<R>(Am, aci, arp, tid, nt, n, sph, ax);
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const int i0 = tid + k * nt;
+        const double ri = i0 < n ? __ldg(bg + i0) - ax[k] : 0.0;
+        for (int l = 0; l < 32; ++l) {
+          const double rl = __shfl_sync(kFull, ri, l);
+          if (k * 32 + l < n) acc = fma(rl, rl, acc);
+        }
+      }
+      if (tid == 0) a.true_res[sys] = sqrt(acc);
+      return;
+    }
     if (Asell)
       rows_acc_sell<R>(Asell, saci, P.sa_off, arp, tid, nt, n, sph, ax);
     else
@@ -630,14 +693,19 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
 #define BILU_RR_BOUNDS __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 : 128)), R == 8 ? 3 : 1)
 
 // one CTA per system of a batch sharing one pattern
-template <int R, int PV, typename FT>
+// REF: the reference's operation order, one warp per system (n <= 256; the
+// plan checks): thread l's rows l, l+32, ... are the reference's lane-strided
+// inner-product terms, and lane 0 of the xor butterfly adds the same pairs as
+// its shfl_down tree (IEEE addition commutes), so every scalar is the
+// reference's bit for bit.
+template <int R, int PV, typename FT, bool REF = false>
 __global__ void BILU_RR_BOUNDS k_bicgstab_rr(const SolveArgs a, const RRLayout L) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int sys = blockIdx.x;
   if (sys >= a.nsys) return;
   const DevPattern& P = a.pat;
-  rr_solve<R, PV, FT, true>(a, P, L, smem, sys, a.A + (size_t)sys * P.a_nnz, a.b + (size_t)sys * P.n,
-                            a.x + (size_t)sys * P.n);
+  rr_solve<R, PV, FT, true, REF>(a, P, L, smem, sys, a.A + (size_t)sys * P.a_nnz, a.b + (size_t)sys * P.n,
+                                 a.x + (size_t)sys * P.n);
 }
 
 // one CTA per system of an uneven-batch bucket (own size and pattern each):
@@ -674,36 +742,17 @@ __global__ void BILU_RR_BOUNDS k_bicgstab_rr_uneven(const UnevenArgs u) {
     P.ilu_prog = u.meta + d.o_ip;
   }
   const RRLayout L = rr_layout_base(d.n, d.nnz, PV, sizeof(FT) == 4, true);
-  rr_solve<R, PV, FT, false>(u.base, P, L, smem, sys, u.base.A + d.val_off, u.base.b + d.vec_off,
-                             u.base.x + d.vec_off);
+  rr_solve<R, PV, FT, false, false>(u.base, P, L, smem, sys, u.base.A + d.val_off, u.base.b + d.vec_off,
+                                    u.base.x + d.vec_off);
 }
 
-template <int R, int PV, typename FT>
-cudaError_t launch_rr_t(const SolveArgs& a, const RRLayout& L, int nt, cudaStream_t st) {
-  auto k = k_bicgstab_rr<R, PV, FT>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total);
-  if (e != cudaSuccess) return e;
-  k<<<a.nsys, nt, L.total, st>>>(a, L);
-  return cudaGetLastError();
-}
-
-template <int PV, typename FT>
+template <int PV, typename FT, bool REF>
 const void* rr_kernel_pv(int R) {
   switch (R) {
-    case 1: return (const void*)k_bicgstab_rr<1, PV, FT>;
-    case 2: return (const void*)k_bicgstab_rr<2, PV, FT>;
-    case 4: return (const void*)k_bicgstab_rr<4, PV, FT>;
-    default: return (const void*)k_bicgstab_rr<8, PV, FT>;
-  }
-}
-
-template <int PV, typename FT>
-cudaError_t launch_rr_pv(const SolveArgs& a, const RRLayout& L, int nt, int R, cudaStream_t st) {
-  switch (R) {
-    case 1: return launch_rr_t<1, PV, FT>(a, L, nt, st);
-    case 2: return launch_rr_t<2, PV, FT>(a, L, nt, st);
-    case 4: return launch_rr_t<4, PV, FT>(a, L, nt, st);
-    default: return launch_rr_t<8, PV, FT>(a, L, nt, st);
+    case 1: return (const void*)k_bicgstab_rr<1, PV, FT, REF>;
+    case 2: return (const void*)k_bicgstab_rr<2, PV, FT, REF>;
+    case 4: return (const void*)k_bicgstab_rr<4, PV, FT, REF>;
+    default: return (const void*)k_bicgstab_rr<8, PV, FT, REF>;
   }
 }
 
@@ -740,21 +789,29 @@ int rr_rows_per_thread(int n, int nt) {
 
 int rr_max_threads(int R) { return R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 : 128)); }
 
-const void* rr_kernel(int pv, int fp32, int R) {
-  if (pv == 0) return rr_kernel_pv<0, double>(R);
-  if (pv == 1) return fp32 ? rr_kernel_pv<1, float>(R) : rr_kernel_pv<1, double>(R);
-  if (pv == 3) return fp32 ? rr_kernel_pv<3, float>(R) : rr_kernel_pv<3, double>(R);
-  return fp32 ? rr_kernel_pv<2, float>(R) : rr_kernel_pv<2, double>(R);
+const void* rr_kernel(int pv, int fp32, int R, int ref) {
+  if (ref) {  // reference order: no preconditioner or ILU factors (one warp per system)
+    if (pv == 0) return rr_kernel_pv<0, double, true>(R);
+    if (pv == 3) return fp32 ? rr_kernel_pv<3, float, true>(R) : rr_kernel_pv<3, double, true>(R);
+    return nullptr;
+  }
+  if (pv == 0) return rr_kernel_pv<0, double, false>(R);
+  if (pv == 1) return fp32 ? rr_kernel_pv<1, float, false>(R) : rr_kernel_pv<1, double, false>(R);
+  if (pv == 3) return fp32 ? rr_kernel_pv<3, float, false>(R) : rr_kernel_pv<3, double, false>(R);
+  return fp32 ? rr_kernel_pv<2, float, false>(R) : rr_kernel_pv<2, double, false>(R);
 }
 
-cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, cudaStream_t st) {
+cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, int ref,
+                            cudaStream_t st) {
   if (a.nsys == 0) return cudaSuccess;
   const int R = rr_rows_per_thread(a.pat.n, nt);
-  if (R == 0 || nt % 32 || nt > rr_max_threads(R)) return cudaErrorInvalidConfiguration;
-  if (pv == 0) return launch_rr_pv<0, double>(a, L, nt, R, st);
-  if (pv == 1) return fp32 ? launch_rr_pv<1, float>(a, L, nt, R, st) : launch_rr_pv<1, double>(a, L, nt, R, st);
-  if (pv == 3) return fp32 ? launch_rr_pv<3, float>(a, L, nt, R, st) : launch_rr_pv<3, double>(a, L, nt, R, st);
-  return fp32 ? launch_rr_pv<2, float>(a, L, nt, R, st) : launch_rr_pv<2, double>(a, L, nt, R, st);
+  if (R == 0 || nt % 32 || nt > rr_max_threads(R) || (ref && nt != 32)) return cudaErrorInvalidConfiguration;
+  const void* k = rr_kernel(pv, fp32, R, ref);
+  if (!k) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total);
+  if (e != cudaSuccess) return e;
+  void* args[] = {const_cast<SolveArgs*>(&a), const_cast<RRLayout*>(&L)};
+  return cudaLaunchKernel(k, dim3(a.nsys), dim3(nt), args, (size_t)L.total, st);
 }
 
 }  // namespace bilu

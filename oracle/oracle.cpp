@@ -699,7 +699,7 @@ ORC_API void orc_bicgstab(int n, int nnz, const int* rp, const int* ci, int nsys
 // recurrences, exits and iteration counting as orc_bicgstab, in this order --
 //   thread partial   fma over the thread's rows in k order, from 0.0
 //   warp             xor butterfly v_l = v_l + v_(l^off), off = 16..1; lane 0
-//   block            0.0 + w_0 + w_1 + ... over the warps in order
+//   block            w_0 + w_1 + ... over the warps in order
 //   rows             A*x and the ISAI rows: fma over the row, from 0.0; ISAI in
 //                    float when fp32 (input rounded, output widened)
 //   LU solve         in-place factors: input rounded to FT; lower rows ascending,
@@ -738,7 +738,7 @@ double fast_block_sum(const std::vector<double>& part, int nt) {
       for (int l = 0; l < 32; ++l) nv[l] = v[l] + v[l ^ off];
       for (int l = 0; l < 32; ++l) v[l] = nv[l];
     }
-    s = s + v[0];
+    s = w == 0 ? v[0] : s + v[0];
   }
   return s;
 }
