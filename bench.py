@@ -95,6 +95,16 @@ def fp64_flops_per_iter(n, nnz, prec_nnz, precond):
     return 2 * fma
 
 
+def launches_per_step(info):
+    """Kernels one headline solve launches: ParILU sweeps, ISAI, the solver, plus one SELL-32 copy each of A
+    and aiU when the plan reads them that way and does not stage them in shared memory."""
+    ops = info["operands_in_smem"]
+    n = 3
+    if ops & 8:
+        n += (0 if ops & 1 else 1) + (0 if ops & 4 else 1)
+    return n
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -581,7 +591,7 @@ def main():
                                   f"no collective on the data path"},
         "clocks": res["clocks"],
         "e2e": res["e2e"],
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": launches_per_step(info) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": RR_TRAFFIC_BYTES_PER_SYSTEM * nsys if info["solver_kernel"] == 1 and fp32_prec
                      else None, "traffic_source": "ncu capture of 3072 systems, scaled per system", "peak_kind": peak_kind, "kernel": "k_bicgstab_rr (register-resident solver)" if info["solver_kernel"] == 1 else "k_bicgstab (solver)",

@@ -157,7 +157,9 @@ typedef struct bilu_plan_info {
   int max_row_len;       /* longest row of the factor pattern                      */
   int threads;           /* CTA size used per system by the solver kernel          */
   int smem_bytes;        /* dynamic shared memory per system of the solver kernel  */
-  int operands_in_smem;  /* bit 0: A, bit 1: factors / aiL, bit 2: aiU in shared memory */
+  int operands_in_smem;  /* bit 0: A, bit 1: factors / aiL, bit 2: aiU in shared memory;
+                            bit 3: A, and aiU, left in global memory are read from SELL-32
+                            copies made by one extra launch each per solve */
   int solver_kernel;     /* 0: one CTA per system, vectors in shared memory (every mode);
                             1: register-resident (BILU_REDUCE_FAST with ISAI or no
                             preconditioner, n <= 2048): `threads` threads per system,

@@ -934,7 +934,8 @@ bilu_status bilu_plan_get_info(const bilu_plan* P, bilu_plan_info* info) {
   if (P->rr) {
     info->threads = P->rr_threads;
     info->smem_bytes = P->rr_lay.total;
-    info->operands_in_smem = (P->rr_lay.A >= 0 ? 1 : 0) | (P->rr_lay.ail >= 0 ? 2 : 0) | (P->rr_lay.aiu >= 0 ? 4 : 0);
+    info->operands_in_smem = (P->rr_lay.A >= 0 ? 1 : 0) | (P->rr_lay.ail >= 0 ? 2 : 0) | (P->rr_lay.aiu >= 0 ? 4 : 0) |
+                             (P->rr_sell ? 8 : 0);
   }
   return BILU_OK;
 }
