@@ -62,8 +62,9 @@ struct DevPattern {
   const int* ail_ci = nullptr;
   const int* aiu_rp = nullptr;
   const int* aiu_ci = nullptr;
-  // program per ISAI row: blocks {t, k} followed by k entries {c, pos}
-  const int* ail_prog_ptr = nullptr;  // n+1 (in int2 units)
+  // program per ISAI row: blocks {t, k} followed by k entries {c, pos}; rows
+  // in blocks of 32, word j of row 32b+l at prog[prog_ptr[b] + 32j + l]
+  const int* ail_prog_ptr = nullptr;  // (n+31)/32 + 1 block offsets (int2 units)
   const int2* ail_prog = nullptr;
   const int* aiu_prog_ptr = nullptr;
   const int2* aiu_prog = nullptr;

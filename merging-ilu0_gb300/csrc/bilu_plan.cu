@@ -517,10 +517,32 @@ bilu_status upload(bilu_plan& P) {
     o_alci = put(P.ail_ci);
     o_aurp = put(P.aiu_rp);
     o_auci = put(P.aiu_ci);
-    o_alpp = put(P.ail_prog_ptr);
-    o_alp = put(P.ail_prog);
-    o_aupp = put(P.aiu_prog_ptr);
-    o_aup = put(P.aiu_prog);
+    // device layout of the per-row ISAI programs: rows in blocks of 32 (a warp's rows), word j of
+    // row 32b+l at off[b] + 32j + l (int2 units), so a warp's program loads are contiguous lines
+    auto blocked = [&](const std::vector<int>& ptr, const std::vector<int>& prog, std::vector<int>& off,
+                       std::vector<int>& words) {
+      const int nb = (P.n + 31) / 32;
+      off.assign(nb + 1, 0);
+      for (int bk = 0; bk < nb; ++bk) {
+        int len = 0;
+        for (int i = 32 * bk; i < std::min(P.n, 32 * bk + 32); ++i) len = std::max(len, ptr[i + 1] - ptr[i]);
+        off[bk + 1] = off[bk] + 32 * len;
+      }
+      words.assign(2 * (size_t)off[nb], 0);
+      for (int i = 0; i < P.n; ++i)
+        for (int j = 0; j < ptr[i + 1] - ptr[i]; ++j) {
+          const size_t dst = 2 * ((size_t)off[i / 32] + 32 * j + i % 32);
+          words[dst] = prog[2 * (ptr[i] + j)];
+          words[dst + 1] = prog[2 * (ptr[i] + j) + 1];
+        }
+    };
+    std::vector<int> off, words;
+    blocked(P.ail_prog_ptr, P.ail_prog, off, words);
+    o_alpp = put(off);
+    o_alp = put(words);
+    blocked(P.aiu_prog_ptr, P.aiu_prog, off, words);
+    o_aupp = put(off);
+    o_aup = put(words);
   }
   cudaError_t e = cudaMalloc((void**)&P.dbuf, buf.size() * sizeof(int));
   if (e != cudaSuccess) return set_error(BILU_ERR_ALLOC, std::string("plan upload: ") + cudaGetErrorString(e));

@@ -233,12 +233,14 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
     const int beg = __ldg(P.ail_rp + i), sz = __ldg(P.ail_rp + i + 1) - beg;
     double* m = M + beg;
     m[sz - 1] = P.l_diag ? 1.0 / LU[__ldg(P.diag + i)] : 1.0;
-    int q = __ldg(P.ail_prog_ptr + i);
+    int q = __ldg(P.ail_prog_ptr + (i >> 5)) + (i & 31);
     for (int blk = 0; blk < sz - 1; ++blk) {
-      const int2 h = __ldg(P.ail_prog + q++);  // {t, count}
+      const int2 h = __ldg(P.ail_prog + q);  // {t, count}; a row's words are 32 apart
+      q += 32;
       double acc = 0.0;
       for (int u = 0; u < h.y; ++u) {
-        const int2 e = __ldg(P.ail_prog + q++);  // {c, position in LU}
+        const int2 e = __ldg(P.ail_prog + q);  // {c, position in LU}
+        q += 32;
         acc = fma(-m[e.x], LU[e.y], acc);
       }
       m[h.x] = P.l_diag ? acc / LU[__ldg(P.diag + __ldg(P.ail_ci + beg + h.x))] : acc;
@@ -257,12 +259,14 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
     const int beg = __ldg(P.aiu_rp + i), sz = __ldg(P.aiu_rp + i + 1) - beg;
     double* m = M + beg;
     m[0] = FAST ? rinv[i] : 1.0 / LU[__ldg(P.diag + i)];
-    int q = __ldg(P.aiu_prog_ptr + i);
+    int q = __ldg(P.aiu_prog_ptr + (i >> 5)) + (i & 31);
     for (int blk = 1; blk < sz; ++blk) {
-      const int2 h = __ldg(P.aiu_prog + q++);
+      const int2 h = __ldg(P.aiu_prog + q);  // {t, count}; a row's words are 32 apart
+      q += 32;
       double acc = 0.0;
       for (int u = 0; u < h.y; ++u) {
-        const int2 e = __ldg(P.aiu_prog + q++);
+        const int2 e = __ldg(P.aiu_prog + q);  // {c, position in LU}
+        q += 32;
         acc = fma(-m[e.x], LU[e.y], acc);
       }
       const int jt = __ldg(P.aiu_ci + beg + h.x);
@@ -296,12 +300,14 @@ __global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, 
     const int beg = __ldg(P.ail_rp + i), sz = __ldg(P.ail_rp + i + 1) - beg;
     float* m = M + beg;
     m[sz - 1] = 1.0f;
-    int q = __ldg(P.ail_prog_ptr + i);
+    int q = __ldg(P.ail_prog_ptr + (i >> 5)) + (i & 31);
     for (int blk = 0; blk < sz - 1; ++blk) {
-      const int2 h = __ldg(P.ail_prog + q++);
+      const int2 h = __ldg(P.ail_prog + q);  // {t, count}; a row's words are 32 apart
+      q += 32;
       float acc = 0.0f;
       for (int u = 0; u < h.y; ++u) {
-        const int2 e = __ldg(P.ail_prog + q++);
+        const int2 e = __ldg(P.ail_prog + q);  // {c, position in LU}
+        q += 32;
         acc = fmaf(-m[e.x], LU[e.y], acc);
       }
       m[h.x] = acc;
@@ -317,12 +323,14 @@ __global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, 
     const int beg = __ldg(P.aiu_rp + i), sz = __ldg(P.aiu_rp + i + 1) - beg;
     float* m = M + beg;
     m[0] = rinv[i];
-    int q = __ldg(P.aiu_prog_ptr + i);
+    int q = __ldg(P.aiu_prog_ptr + (i >> 5)) + (i & 31);
     for (int blk = 1; blk < sz; ++blk) {
-      const int2 h = __ldg(P.aiu_prog + q++);
+      const int2 h = __ldg(P.aiu_prog + q);  // {t, count}; a row's words are 32 apart
+      q += 32;
       float acc = 0.0f;
       for (int u = 0; u < h.y; ++u) {
-        const int2 e = __ldg(P.aiu_prog + q++);
+        const int2 e = __ldg(P.aiu_prog + q);  // {c, position in LU}
+        q += 32;
         acc = fmaf(-m[e.x], LU[e.y], acc);
       }
       m[h.x] = acc * rinv[__ldg(P.aiu_ci + beg + h.x)];
