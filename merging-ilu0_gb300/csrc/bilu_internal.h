@@ -243,7 +243,7 @@ __host__ __device__ inline RRLayout rr_layout_base(int n, int nnz, int pv, bool 
     dst = off;
     off = (int)((off + bytes + 15) & ~15LL);
   };
-  take(L.red, 4 * 64 * 8);
+  take(L.red, (4 * 64 + 16) * 8);  // four reduction slots and the broadcast scalars
   take(L.ph, (long long)n * 8);
   if (pv == 1 || pv == 2 || (pv == 3 && fp32)) take(L.in, (long long)n * fts);
   if (pv == 1) take(L.mid, (long long)n * fts);

@@ -22,9 +22,11 @@
 //     s_hat (FP64), the preconditioner input and intermediate (FT), and, when
 //     they fit without costing occupancy, A and the ISAI values;
 //   * the six inner products of an iteration run as four block reductions
-//     (xor-butterfly within each warp, then every thread sums the per-warp
-//     partials in warp order), so all threads hold identical scalars and take
-//     identical branches without a broadcast barrier; 9 barriers per iteration;
+//     (xor-butterfly within each warp, then warp 0 sums the per-warp partials
+//     in warp order); warp 0 alone forms the scalar recurrence (divisions,
+//     square roots, the next beta) and broadcasts it through shared memory, so
+//     those FP64 instructions run once per CTA, not once per warp; 13
+//     barriers per iteration;
 //   * the CTA is small (one warp for n <= 256), so several systems share an SM
 //     and one system's barrier or reduction latency overlaps another's FMAs;
 //   * with FP32 ISAI values (BILU_FP32) both preconditioner SpMVs run on the
@@ -78,6 +80,33 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* red, int nw) {
     for (int w = 1; w < nw; ++w) s = s + red[k * 32 + w];
     v[k] = s;
   }
+}
+
+// block_sum for warp 0 only: the same sums in the same order land in warp 0's
+// threads (the other warps' v is left as it was); returns true on warp 0.
+// Warp 0 then forms the scalar recurrence alone and broadcasts it, so the
+// divisions and square roots of an iteration run once per CTA, not per warp.
+template <int K>
+__device__ __forceinline__ bool block_sum_w0(double (&v)[K], double* red, int nw) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v[k] = v[k] + __shfl_xor_sync(kFull, v[k], off);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) red[k * 32 + warp] = v[k];
+  }
+  __syncthreads();
+  if (warp != 0) return false;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double s = red[k * 32];
+    for (int w = 1; w < nw; ++w) s = s + red[k * 32 + w];
+    v[k] = s;
+  }
+  return true;
 }
 
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
@@ -368,7 +397,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
   const auto* __restrict__ saci = pick_ci<C16>(P.sa_ci16, P.sa_ci);
   const auto* __restrict__ suci = pick_ci<C16>(P.su_ci16, P.su_ci);
 
-  double* red = reinterpret_cast<double*>(smem + L.red);  // 4 slots of 2 * 32
+  double* red = reinterpret_cast<double*>(smem + L.red);  // 4 slots of 2 * 32, then 16 broadcast scalars
   double* sph = reinterpret_cast<double*>(smem + L.ph);
   FT* sin = reinterpret_cast<FT*>(smem + L.in);
   FT* smid = reinterpret_cast<FT*>(smem + L.mid);
@@ -470,11 +499,18 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     if (i < n) q[0] = fma(bi, bi, q[0]);
   }
   // ||b||^2 = (r, r_hat) at the start: one reduction serves both (its barrier
-  // also completes the staging above)
-  block_sum<1>(q, red, nw);
-  const double bnorm = sqrt(q[0]);
+  // also completes the staging above).  bc: the scalars warp 0 broadcasts.
+  double* bc = red + 256;
+  const bool lane0 = (tid & 31) == 0;
+  if (block_sum_w0<1>(q, red, nw) && lane0) {
+    bc[0] = sqrt(q[0]);
+    bc[1] = q[0];
+  }
+  __syncthreads();
+  const double bnorm = bc[0];
   const double thr = (a.tol_mode == BILU_TOL_ABS) ? a.tol : a.tol * bnorm;
-  double rho = q[0], rho_old = 1.0, alpha = 1.0, omega_old = 1.0, res = bnorm;
+  double rho = bc[1], rho_old = 1.0, alpha = 1.0, omega_old = 1.0, res = bnorm;
+  double beta = (rho / rho_old) * (alpha / omega_old);  // the first iteration's; warp 0 forms the later ones
   float iter = 0.0f;
   int status = BILU_SYS_MAX_ITER;
   bool stop = false;
@@ -541,7 +577,6 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
       status = BILU_SYS_BREAKDOWN_RHO;
       break;
     }
-    const double beta = (rho / rho_old) * (alpha / omega_old);
 #pragma unroll
     for (int k = 0; k < R; ++k) p[k] = fma(beta, fma(-omega_old, v[k], p[k]), r[k]);
     BILU_RR_INPUT(p);
@@ -560,8 +595,9 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
       const int i = tid + k * nt;
       if (i < n) q[0] = fma(__ldg(bg + i), v[k], q[0]);
     }
-    block_sum<1>(q, red + 64, nw);
-    alpha = rho / q[0];
+    if (block_sum_w0<1>(q, red + 64, nw) && lane0) bc[2] = rho / q[0];
+    __syncthreads();
+    alpha = bc[2];
     // x += alpha p_hat, s = r - alpha v, ||s||.  p_hat is read before anyone
     // rewrites sph (PV 0 rewrites it with s right here, after the reduction's
     // barrier has ended every SpMV read).
@@ -576,8 +612,9 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
       }
     }
     BILU_RR_INPUT(r);
-    block_sum<1>(q, red + 128, nw);
-    res = sqrt(q[0]);
+    if (block_sum_w0<1>(q, red + 128, nw) && lane0) bc[3] = sqrt(q[0]);
+    __syncthreads();
+    res = bc[3];
     iter = iter + 0.5f;
     if (res < thr) {
       status = BILU_SYS_CONVERGED;
@@ -600,8 +637,9 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
         q2[1] = fma(t[k], t[k], q2[1]);
       }
     }
-    block_sum<2>(q2, red + 192, nw);
-    const double omega = q2[0] / q2[1];
+    if (block_sum_w0<2>(q2, red + 192, nw) && lane0) bc[4] = q2[0] / q2[1];
+    __syncthreads();
+    const double omega = bc[4];
     // x += omega s_hat, r = s - omega t, ||r||, next rho = (r, r_hat)
     q2[0] = 0.0;
     q2[1] = 0.0;
@@ -615,12 +653,17 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
         q2[1] = fma(__ldg(bg + i), r[k], q2[1]);
       }
     }
-    block_sum<2>(q2, red, nw);
-    res = sqrt(q2[0]);
+    if (block_sum_w0<2>(q2, red, nw) && lane0) {
+      bc[5] = sqrt(q2[0]);
+      bc[6] = q2[1];
+      bc[7] = (q2[1] / rho) * (alpha / omega);  // the next iteration's beta: (rho_new / rho_old) * (alpha / omega_old)
+    }
+    __syncthreads();
+    res = bc[5];
     iter = iter + 0.5f;
-    rho_old = rho;
     omega_old = omega;
-    rho = q2[1];
+    rho = bc[6];
+    beta = bc[7];
     if (res < thr) {
       status = BILU_SYS_CONVERGED;
       break;
