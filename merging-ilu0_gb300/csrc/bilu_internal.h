@@ -232,10 +232,15 @@ struct RRLayout {
   int red = -1, ph = -1, in = -1, mid = -1, F = -1, rinv = -1, A = -1, ail = -1, aiu = -1, total = 0;
 };
 
-// The mandatory part of an RRLayout (no optional staging), the same on host
-// and device: pv 0 none, 1 two-triangle ISAI, 2 general ISAI, 3 ILU factors
-// (inkernel: the FP64 factorisation slot of the merged form).
-__host__ __device__ inline RRLayout rr_layout_base(int n, int nnz, int pv, bool fp32, bool inkernel) {
+// Bytes of the reduction slot of an nt-thread CTA: two partial sums per
+// thread and 16 broadcast scalars.
+__host__ __device__ inline int rr_red_bytes(int nt) { return (2 * nt + 16) * 8; }
+
+// The mandatory part of an RRLayout (no optional staging) for nt threads, the
+// same on host and device: pv 0 none, 1 two-triangle ISAI, 2 general ISAI, 3
+// ILU factors (inkernel: the FP64 factorisation slot of the merged form).  The
+// reduction slot comes first, so the rest of the layout does not depend on nt.
+__host__ __device__ inline RRLayout rr_layout_base(int n, int nnz, int pv, bool fp32, bool inkernel, int nt) {
   RRLayout L;
   int off = 0;
   const int fts = fp32 ? 4 : 8;
@@ -243,7 +248,7 @@ __host__ __device__ inline RRLayout rr_layout_base(int n, int nnz, int pv, bool 
     dst = off;
     off = (int)((off + bytes + 15) & ~15LL);
   };
-  take(L.red, (4 * 64 + 16) * 8);  // four reduction slots and the broadcast scalars
+  take(L.red, rr_red_bytes(nt));
   take(L.ph, (long long)n * 8);
   if (pv == 1 || pv == 2 || (pv == 3 && fp32)) take(L.in, (long long)n * fts);
   if (pv == 1) take(L.mid, (long long)n * fts);

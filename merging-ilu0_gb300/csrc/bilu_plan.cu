@@ -415,7 +415,7 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   const int fts = fp32 ? 4 : 8;
   if (pv == 3 && P.tp_lo.empty()) return false;
   // the merged form factorises in FP64 in the factor slot before rounding to FT
-  RRLayout L = rr_layout_base(n, P.nnz, pv, fp32, pk == PK_ILU_INKERNEL);
+  RRLayout L = rr_layout_base(n, P.nnz, pv, fp32, pk == PK_ILU_INKERNEL, nt);
   int off = L.total;
   auto take = [&](int& dst, long long bytes) {
     dst = off;

@@ -39,6 +39,7 @@ struct Bucket {
   int maxn = 0;
   bool rr = false;           // register-resident solver, one CTA per system (FAST order, n <= 1024)
   int R = 0;                 // its rows per thread
+  int rr_rest = 0;           // its largest layout without the reduction slot (which depends on the CTA size)
 };
 
 }  // namespace
@@ -109,9 +110,12 @@ int rr_pv(const bilu_options& o) { return o.precond == BILU_PRECOND_NONE ? 0 : 3
 bool rr_setup(const bilu_uneven_plan* U, Bucket& b, int nt) {
   const int R = rr_rows_per_thread(b.maxn, nt);
   if (R == 0 || nt % 32 || nt > rr_max_threads(R)) return false;
+  b.smem = rr_red_bytes(nt) + b.rr_rest;
+  if (b.smem > (int)solve_max_smem()) return false;
   const void* k = rr_uneven_kernel(rr_pv(U->opts), U->opts.factor_precision == BILU_FP32, R);
   int occ = 0;
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, b.smem) != cudaSuccess ||
+  // buckets can share a kernel with different layouts: allow the device maximum, launch with b.smem
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)solve_max_smem()) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, nt, b.smem) != cudaSuccess || occ < 1) {
     cudaGetLastError();
     return false;
@@ -168,7 +172,10 @@ bilu_status capture(bilu_uneven_plan* U, const double* vals, const double* rhs, 
     const void* k = b.rr ? rr_uneven_kernel(rr_pv(U->opts), U->opts.factor_precision == BILU_FP32, b.R)
                          : uneven_kernel(U->opts.factor_precision == BILU_FP32, U->opts.reduction == BILU_REDUCE_FAST,
                                          b.maxl);
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, b.smem);
+    // register-resident buckets can share a kernel with different layouts: allow the device maximum
+    // (the kernel has no static shared memory) and launch with b.smem; the persistent kernel keeps b.smem
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         b.rr ? (int)solve_max_smem() : b.smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
   }
   cudaError_t e = cudaStreamBeginCapture(U->cap, cudaStreamCaptureModeThreadLocal);
@@ -362,13 +369,11 @@ bilu_status bilu_uneven_plan_create(bilu_uneven_plan** out, int nsys, const int*
     }
     // FAST order: the register-resident solver's layout for every system of the bucket
     if (fast && !b.sys.empty() && b.maxn <= 1024) {
-      int rsm = 0;
+      int rest = 0;
       for (int s : b.sys)
-        rsm = std::max(rsm, rr_layout_base(h_sys_n[s], h_sys_nnz[s], rr_pv(o), fp32, true).total);
-      if (rsm <= budget) {
-        b.rr = true;
-        b.smem = rsm;
-      }
+        rest = std::max(rest, rr_layout_base(h_sys_n[s], h_sys_nnz[s], rr_pv(o), fp32, true, 0).total - rr_red_bytes(0));
+      b.rr = true;
+      b.rr_rest = rest;  // rr_setup checks the total for its CTA size
     }
     if (b.smem > budget) {
       const int need = b.smem;
@@ -450,7 +455,7 @@ bilu_status bilu_uneven_autotune(bilu_uneven_plan* U, const double* d_values, co
   for (int bi = 0; bi < (int)U->buckets.size() && !res; ++bi) {
     Bucket& b = U->buckets[bi];
     if (b.sys.empty()) continue;
-    int best_t = b.threads, best_g = b.grid, best_R = b.R;
+    int best_t = b.threads, best_g = b.grid;
     float best = 1e30f;
     const int rr_base = round32((b.maxn + 7) / 8);
     const int rr_cands[] = {rr_base, 2 * rr_base, 4 * rr_base, 0, 0};
@@ -466,7 +471,7 @@ bilu_status bilu_uneven_autotune(bilu_uneven_plan* U, const double* d_values, co
         trial.threads = t;
         trial.grid = g;
       }
-      const int g = trial.grid, tR = trial.R;
+      const int g = trial.grid;
       std::swap(U->buckets[bi], trial);
       float ms_min = 1e30f;
       for (int rep = 0; rep < 2 && !res; ++rep) {
@@ -485,12 +490,14 @@ bilu_status bilu_uneven_autotune(bilu_uneven_plan* U, const double* d_values, co
         best = ms_min;
         best_t = t;
         best_g = g;
-        best_R = tR;
       }
     }
-    b.threads = best_t;
-    b.grid = best_g;
-    b.R = best_R;
+    if (b.rr) {
+      rr_setup(U, b, best_t);  // threads, rows per thread, grid and shared memory of the winner
+    } else {
+      b.threads = best_t;
+      b.grid = best_g;
+    }
     b.tuned_ms = best;
   }
   cudaEventDestroy(e0);

@@ -38,8 +38,10 @@
 //
 // Reduction order (what orc_bicgstab_fast restates):
 //   thread partial   d = fma(a_i, b_i, d) over its rows in k order, from 0.0
-//   warp             lane values v_l; for off = 16, 8, 4, 2, 1: v_l = v_l + v_(l^off); lane 0's value
-//   block            s = w_0; s = s + w_j for warps j = 1 .. NT/32-1
+//   no ILU factors   lane l: s_l = d_l; s_l = s_l + d_(l+32j) for warps j = 1 .. NT/32-1,
+//                    then for off = 16, 8, 4, 2, 1: s_l = s_l + s_(l^off); lane 0's value
+//   ILU factors      per warp: for off = 16 .. 1: d_l = d_l + d_(l^off), lane 0's value
+//                    w_j; then s = w_0 + w_1 + ... over the warps in order
 //   SpMV row         acc = fma(a_k, x_ci(k), acc), k ascending, from 0.0 (FP64)
 //   ISAI row (FT)    the same in FT; input rounded to FT, output widened to FP64
 //   LU solve (FT)    input rounded to FT; lower row i: a = y_i, a = fma(-l_ik, y_k, a)
@@ -59,52 +61,46 @@ constexpr unsigned kFull = 0xffffffffu;
 #include "k_ilu_rows.cuh"
 #include "k_row_ref.cuh"
 
-// K values summed over the CTA; every thread returns the same sums.
-// red: K * 32 doubles of this reduction's own slot.
-template <int K>
-__device__ __forceinline__ void block_sum(double (&v)[K], double* red, int nw) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) v[k] = v[k] + __shfl_xor_sync(kFull, v[k], off);
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) red[k * 32 + warp] = v[k];
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    double s = red[k * 32];
-    for (int w = 1; w < nw; ++w) s = s + red[k * 32 + w];
-    v[k] = s;
-  }
-}
-
-// block_sum for warp 0 only: the same sums in the same order land in warp 0's
-// threads (the other warps' v is left as it was); returns true on warp 0.
-// Warp 0 then forms the scalar recurrence alone and broadcasts it, so the
-// divisions and square roots of an iteration run once per CTA, not per warp.
-template <int K>
+// K values summed over the CTA into the threads of warp 0 (the other warps'
+// v is left as it was); returns true on warp 0, which then forms the scalar
+// recurrence alone and broadcasts it, so the divisions and square roots of an
+// iteration run once per CTA.  Two orders (red: K * nt doubles):
+//   LANES_FIRST  every thread stores its partial; lane l of warp 0 sums
+//                partials l, l+32, l+64, ... in order, then an xor butterfly
+//                (v_l = v_l + v_(l^off), off = 16 .. 1).  Only warp 0 adds.
+//   otherwise    an xor butterfly in every warp, lane 0 stores the warp's sum,
+//                and warp 0 sums the warps' sums in order.  Fewer dependent
+//                adds after the barrier: better where barriers are on the
+//                critical path (ILU factors, level-scheduled solves).
+template <int K, bool LANES_FIRST>
 __device__ __forceinline__ bool block_sum_w0(double (&v)[K], double* red, int nw) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nt = nw * 32;
+  if (LANES_FIRST) {
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
+    for (int k = 0; k < K; ++k) red[k * nt + threadIdx.x] = v[k];
+  } else {
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) v[k] = v[k] + __shfl_xor_sync(kFull, v[k], off);
-  }
-  if (lane == 0) {
+    for (int k = 0; k < K; ++k) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) red[k * 32 + warp] = v[k];
+      for (int off = 16; off >= 1; off >>= 1) v[k] = v[k] + __shfl_xor_sync(kFull, v[k], off);
+      if (lane == 0) red[k * nt + warp] = v[k];
+    }
   }
   __syncthreads();
   if (warp != 0) return false;
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    double s = red[k * 32];
-    for (int w = 1; w < nw; ++w) s = s + red[k * 32 + w];
-    v[k] = s;
+    if (LANES_FIRST) {
+      double s = red[k * nt + lane];
+      for (int w = 1; w < nw; ++w) s = s + red[k * nt + w * 32 + lane];
+#pragma unroll
+      for (int off = 16; off >= 1; off >>= 1) s = s + __shfl_xor_sync(kFull, s, off);
+      v[k] = s;
+    } else {
+      double s = red[k * nt];
+      for (int w = 1; w < nw; ++w) s = s + red[k * nt + w];
+      v[k] = s;
+    }
   }
   return true;
 }
@@ -397,7 +393,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
   const auto* __restrict__ saci = pick_ci<C16>(P.sa_ci16, P.sa_ci);
   const auto* __restrict__ suci = pick_ci<C16>(P.su_ci16, P.su_ci);
 
-  double* red = reinterpret_cast<double*>(smem + L.red);  // 4 slots of 2 * 32, then 16 broadcast scalars
+  double* red = reinterpret_cast<double*>(smem + L.red);  // 2 partials per thread, then 16 broadcast scalars
   double* sph = reinterpret_cast<double*>(smem + L.ph);
   FT* sin = reinterpret_cast<FT*>(smem + L.in);
   FT* smid = reinterpret_cast<FT*>(smem + L.mid);
@@ -500,9 +496,9 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
   }
   // ||b||^2 = (r, r_hat) at the start: one reduction serves both (its barrier
   // also completes the staging above).  bc: the scalars warp 0 broadcasts.
-  double* bc = red + 256;
+  double* bc = red + 2 * nt;
   const bool lane0 = (tid & 31) == 0;
-  if (block_sum_w0<1>(q, red, nw) && lane0) {
+  if (block_sum_w0<1, PV != 3>(q, red, nw) && lane0) {
     bc[0] = sqrt(q[0]);
     bc[1] = q[0];
   }
@@ -595,7 +591,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
       const int i = tid + k * nt;
       if (i < n) q[0] = fma(__ldg(bg + i), v[k], q[0]);
     }
-    if (block_sum_w0<1>(q, red + 64, nw) && lane0) bc[2] = rho / q[0];
+    if (block_sum_w0<1, PV != 3>(q, red, nw) && lane0) bc[2] = rho / q[0];
     __syncthreads();
     alpha = bc[2];
     // x += alpha p_hat, s = r - alpha v, ||s||.  p_hat is read before anyone
@@ -612,7 +608,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
       }
     }
     BILU_RR_INPUT(r);
-    if (block_sum_w0<1>(q, red + 128, nw) && lane0) bc[3] = sqrt(q[0]);
+    if (block_sum_w0<1, PV != 3>(q, red, nw) && lane0) bc[3] = sqrt(q[0]);
     __syncthreads();
     res = bc[3];
     iter = iter + 0.5f;
@@ -637,7 +633,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
         q2[1] = fma(t[k], t[k], q2[1]);
       }
     }
-    if (block_sum_w0<2>(q2, red + 192, nw) && lane0) bc[4] = q2[0] / q2[1];
+    if (block_sum_w0<2, PV != 3>(q2, red, nw) && lane0) bc[4] = q2[0] / q2[1];
     __syncthreads();
     const double omega = bc[4];
     // x += omega s_hat, r = s - omega t, ||r||, next rho = (r, r_hat)
@@ -653,7 +649,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
         q2[1] = fma(__ldg(bg + i), r[k], q2[1]);
       }
     }
-    if (block_sum_w0<2>(q2, red, nw) && lane0) {
+    if (block_sum_w0<2, PV != 3>(q2, red, nw) && lane0) {
       bc[5] = sqrt(q2[0]);
       bc[6] = q2[1];
       bc[7] = (q2[1] / rho) * (alpha / omega);  // the next iteration's beta: (rho_new / rho_old) * (alpha / omega_old)
@@ -728,8 +724,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
         q[0] = fma(ri, ri, q[0]);
       }
     }
-    block_sum<1>(q, red + 64, nw);
-    if (tid == 0) a.true_res[sys] = sqrt(q[0]);
+    if (block_sum_w0<1, PV != 3>(q, red, nw) && tid == 0) a.true_res[sys] = sqrt(q[0]);
   }
 }
 
@@ -784,7 +779,7 @@ __global__ void BILU_RR_BOUNDS k_bicgstab_rr_uneven(const UnevenArgs u) {
     P.ilu_hdr = reinterpret_cast<const int4*>(u.meta + d.o_ih);
     P.ilu_prog = u.meta + d.o_ip;
   }
-  const RRLayout L = rr_layout_base(d.n, d.nnz, PV, sizeof(FT) == 4, true);
+  const RRLayout L = rr_layout_base(d.n, d.nnz, PV, sizeof(FT) == 4, true, blockDim.x);
   rr_solve<R, PV, FT, false, false>(u.base, P, L, smem, sys, u.base.A + d.val_off, u.base.b + d.vec_off,
                                     u.base.x + d.vec_off);
 }

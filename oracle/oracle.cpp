@@ -697,9 +697,10 @@ ORC_API void orc_bicgstab(int n, int nnz, const int* rp, const int* ci, int nsys
 // BILU_REDUCE_FAST BiCGSTAB of the register-resident kernel (k_solve_rr.cu)
 // with `nt` threads per system, thread t owning rows t + k*nt: the same
 // recurrences, exits and iteration counting as orc_bicgstab, in this order --
-//   thread partial   fma over the thread's rows in k order, from 0.0
-//   warp             xor butterfly v_l = v_l + v_(l^off), off = 16..1; lane 0
-//   block            w_0 + w_1 + ... over the warps in order
+//   thread partial   d_t = fma over thread t's rows in k order, from 0.0
+//   no ILU factors   lane l: s_l = d_l + d_(l+32) + d_(l+64) + ... in order, then
+//                    xor butterfly s_l = s_l + s_(l^off), off = 16..1; lane 0
+//   ILU factors      xor butterfly per warp (lane 0: w_j), then w_0 + w_1 + ...
 //   rows             A*x and the ISAI rows: fma over the row, from 0.0; ISAI in
 //                    float when fp32 (input rounded, output widened)
 //   LU solve         in-place factors: input rounded to FT; lower rows ascending,
@@ -729,15 +730,26 @@ inline void trsv_lu_fast(int n, const int* rp, const int* ci, const int* diag, c
   }
 }
 
-double fast_block_sum(const std::vector<double>& part, int nt) {
-  double s = 0.0;
-  for (int w = 0; w < nt / 32; ++w) {
-    double v[32], nv[32];
-    for (int l = 0; l < 32; ++l) v[l] = part[32 * w + l];
+double fast_block_sum(const std::vector<double>& part, int nt, bool lanes_first) {
+  double v[32], nv[32];
+  auto butterfly = [&]() {
     for (int off = 16; off >= 1; off >>= 1) {
       for (int l = 0; l < 32; ++l) nv[l] = v[l] + v[l ^ off];
       for (int l = 0; l < 32; ++l) v[l] = nv[l];
     }
+  };
+  if (lanes_first) {
+    for (int l = 0; l < 32; ++l) {
+      v[l] = part[l];
+      for (int w = 1; w < nt / 32; ++w) v[l] = v[l] + part[32 * w + l];
+    }
+    butterfly();
+    return v[0];
+  }
+  double s = 0.0;
+  for (int w = 0; w < nt / 32; ++w) {
+    for (int l = 0; l < 32; ++l) v[l] = part[32 * w + l];
+    butterfly();
     s = w == 0 ? v[0] : s + v[0];
   }
   return s;
@@ -795,7 +807,7 @@ ORC_API int orc_bicgstab_fast(int n, int nnz, const int* rp, const int* ci, int 
         }
         part[th] = d;
       }
-      return fast_block_sum(part, nt);
+      return fast_block_sum(part, nt, pv != 3);
     };
     // z = M in into sph
     auto apply = [&](const std::vector<double>& in) {
