@@ -224,10 +224,10 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
   const int sys = blockIdx.x;
   if (sys >= nsys) return;
   const int n = P.n, nnz = P.nnz;
-  double* LU = reinterpret_cast<double*>(smem);
-  double* M = LU + nnz;  // max(ail_nnz, aiu_nnz)
-  for (int k = threadIdx.x; k < nnz; k += blockDim.x) LU[k] = __ldg(LUg + (size_t)sys * nnz + k);
-  __syncthreads();
+  // the factors are read through L1: only the ISAI values being solved for
+  // occupy shared memory (two CTAs per SM at n = 1000 instead of one)
+  const double* __restrict__ LU = LUg + (size_t)sys * nnz;
+  double* M = reinterpret_cast<double*>(smem);  // max(ail_nnz, aiu_nnz)
   // ---- aiL
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const int beg = __ldg(P.ail_rp + i), sz = __ldg(P.ail_rp + i + 1) - beg;
@@ -507,7 +507,9 @@ cudaError_t launch_isai(const DevPattern& p, int nsys, const double* lu, void* a
                         cudaStream_t st, int fast) {
   if (nsys == 0) return cudaSuccess;
   const bool f32 = fp32 && fast && !p.l_diag;  // FAST FP32 ISAI: computed in FP32 (k_isai_f32)
-  const int smem = (p.nnz + (p.ail_nnz > p.aiu_nnz ? p.ail_nnz : p.aiu_nnz) + (fast ? p.n : 0)) * (f32 ? 4 : 8);
+  // k_isai_f32 stages the factors rounded to float; k_isai reads the FP64 factors through L1
+  const int smem = ((f32 ? p.nnz : 0) + (p.ail_nnz > p.aiu_nnz ? p.ail_nnz : p.aiu_nnz) + (fast ? p.n : 0)) *
+                   (f32 ? 4 : 8);
   void* k = f32 ? (void*)k_isai_f32
                 : fp32 ? (fast ? (void*)k_isai<float, true> : (void*)k_isai<float, false>)
                        : (fast ? (void*)k_isai<double, true> : (void*)k_isai<double, false>);

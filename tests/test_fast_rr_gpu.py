@@ -270,3 +270,27 @@ def test_rr_lu_levels_wider_than_cta(cuda, fp32, precond):
     o = _oracle_fast(rp, ci, v, b, precond, 128, fp32, approach=kw["ilu_approach"], **TOL)
     _check(g, o, f"wide levels precond {precond} fp32={fp32}")
     assert np.all(g["conv"] == 1)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 33])
+@pytest.mark.parametrize("reduction", [bilu.REDUCE_REF, bilu.REDUCE_FAST])
+def test_rr_tiny_systems(cuda, n, reduction):
+    """Systems of 1 to 33 rows (one or two slots of 32 rows, single-level solves) on the register-resident
+    kernel, in both orders, merged ILU(0): bit for bit against the oracle."""
+    rng = np.random.default_rng(n)
+    nsys = 5
+    rows = [sorted({min(max(i + d, 0), n - 1) for d in (-3, -1, 0, 1, 2)}) for i in range(n)]
+    rp = np.zeros(n + 1, np.int32)
+    rp[1:] = np.cumsum([len(r) for r in rows])
+    ci = np.concatenate([np.array(r, np.int32) for r in rows])
+    v = np.where(np.concatenate([np.array(r) == i for i, r in enumerate(rows)])[None, :],
+                 3.0 + rng.random((nsys, len(ci))), -rng.random((nsys, len(ci))))
+    b = rng.uniform(-1, 1, (nsys, n))
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0, reduction=reduction, **TOL)
+    assert g["info"]["solver_kernel"] == 1 and g["info"]["threads"] == 32
+    if reduction == bilu.REDUCE_FAST:
+        o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_ILU0, 32, False, approach=1, **TOL)
+    else:
+        o = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_ILU0, **TOL)
+    _check(g, o, f"n={n} reduction={reduction}")
+    assert np.all(g["conv"] == 1)
