@@ -100,6 +100,7 @@ struct DevPattern {
   // Every level has at least kIluPrefetch + 1 words per slot.
   const int4* ilu_hdr = nullptr;
   const int* ilu_prog = nullptr;
+  int ilu_prog_approach = 0;  // the approach (1..4) whose pair order the program holds
   // 16-bit copies of the column indices read by the register-resident solver's
   // SpMVs (n <= 65535): half the L1 footprint of the int32 arrays
   const unsigned short* a_ci16 = nullptr;

@@ -593,6 +593,7 @@ bilu_status upload(bilu_plan& P) {
   if (!P.ilu_prog.empty()) {
     d.ilu_hdr = reinterpret_cast<const int4*>(b + o_ih);
     d.ilu_prog = b + o_ip;
+    d.ilu_prog_approach = P.opts.ilu_approach;
   }
   if (!P.sa_off.empty()) {
     d.sa_nnz = P.sa_off.back();

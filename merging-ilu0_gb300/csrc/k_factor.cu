@@ -33,6 +33,9 @@ __global__ void k_expand(const int* __restrict__ src, int nnz, int nnz_in, int n
 
 // ---------------------------------------------------------------- ILU(0)
 // Same per-entry arithmetic as the solver kernel's in-kernel factorisation.
+// (The ILU program of the register-resident solver measured 5-15 % slower
+// here: this kernel's small CTAs hide the metadata latency by occupancy, and
+// the prefetched program words cost it registers.)
 __global__ void __launch_bounds__(512) k_ilu0(const DevPattern P, int nsys, const double* __restrict__ A,
                                               double* __restrict__ LUout, int approach) {
   extern __shared__ __align__(16) unsigned char smem[];
