@@ -1,6 +1,9 @@
 // Register-resident batched BiCGSTAB for BILU_REDUCE_FAST with an ISAI
 // preconditioner (two triangles or the general ISAI of A), in-place ILU
-// factors (factorised in the kernel, the merged form, or given) or none.
+// factors (factorised in the kernel, the merged form, or given) or none; and,
+// for n <= 256, ILU factors or none in the reference's operation order (REF:
+// one warp per system; the variant's comment at k_bicgstab_rr says why that
+// order is the reference's).
 //
 // Same method, exits and iteration counting as the shared-memory kernel
 // (k_solve.cu, after PrecondBiCGSTAB_exact_ilu0_app1_merged_gpu.cu:249-538,
@@ -22,19 +25,20 @@
 //     s_hat (FP64), the preconditioner input and intermediate (FT), and, when
 //     they fit without costing occupancy, A and the ISAI values;
 //   * the six inner products of an iteration run as four block reductions
-//     (xor-butterfly within each warp, then warp 0 sums the per-warp partials
-//     in warp order); warp 0 alone forms the scalar recurrence (divisions,
-//     square roots, the next beta) and broadcasts it through shared memory, so
-//     those FP64 instructions run once per CTA, not once per warp; 13
-//     barriers per iteration;
+//     in one shared slot (orders below); warp 0 alone forms the scalar
+//     recurrence (divisions, square roots, the next beta) and broadcasts it
+//     through shared memory, so those FP64 instructions run once per CTA, not
+//     once per warp; 13 barriers per iteration besides the preconditioner's;
 //   * the CTA is small (one warp for n <= 256), so several systems share an SM
 //     and one system's barrier or reduction latency overlaps another's FMAs;
 //   * with FP32 ISAI values (BILU_FP32) both preconditioner SpMVs run on the
 //     FP32 pipe; FP64 stays in A*x, the inner products and the recurrences;
-//   * ILU factors live in shared memory (the merged form factorises there,
-//     rows in level order as the shared-memory kernel does); the triangular
-//     solves run level by level over the whole CTA, in place on the
-//     preconditioner vector, one barrier per level.
+//   * ILU factors live in shared memory (the merged form factorises there
+//     from the plan's ILU program); the triangular solves run level by level
+//     over the whole CTA from the plan's per-level solve programs, in place on
+//     the preconditioner vector, one barrier per level;
+//   * SpMV column indices are read as 16-bit copies, and A and aiU optionally
+//     from SELL-32 copies (coalesced per warp) made before the launch.
 //
 // Reduction order (what orc_bicgstab_fast restates):
 //   thread partial   d = fma(a_i, b_i, d) over its rows in k order, from 0.0
