@@ -109,7 +109,11 @@ typedef struct bilu_options {
                                 through L1.  Operands that do not fit are left out.
                                 Bit 3: A and aiU left in global memory are read from
                                 SELL-32 copies made before the solver launch (same
-                                arithmetic; the copies live in the plan's workspace).     */
+                                arithmetic; the copies live in the plan's workspace).
+                                Bit 4: the kernel variant with 4 CTAs of 128 threads per
+                                SM (128 registers per thread instead of 168; same
+                                arithmetic), taken for 8 rows per thread without ILU
+                                factors and ignored otherwise.                            */
 } bilu_options;
 
 /* Fills *opts with the reference defaults: merged ILU(0), approach 1, 5 sweeps,
@@ -159,10 +163,12 @@ typedef struct bilu_plan_info {
   int smem_bytes;        /* dynamic shared memory per system of the solver kernel  */
   int operands_in_smem;  /* bit 0: A, bit 1: factors / aiL, bit 2: aiU in shared memory;
                             bit 3: A, and aiU, left in global memory are read from SELL-32
-                            copies made by one extra launch each per solve */
+                            copies made by one extra launch each per solve; bit 4: the
+                            4-CTAs-per-SM variant of the register-resident kernel */
   int solver_kernel;     /* 0: one CTA per system, vectors in shared memory (every mode);
-                            1: register-resident (BILU_REDUCE_FAST with ISAI or no
-                            preconditioner, n <= 2048): `threads` threads per system,
+                            1: register-resident (BILU_REDUCE_FAST with n <= 1024, or
+                            the reference order with n <= 256, ILU factors or none and
+                            rows of at most 16 entries): `threads` threads per system,
                             each owning rows t + k * threads                         */
 } bilu_plan_info;
 bilu_status bilu_plan_get_info(const bilu_plan* plan, bilu_plan_info* info);

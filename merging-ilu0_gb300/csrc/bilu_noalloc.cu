@@ -186,7 +186,7 @@ extern "C" bilu_status bilu_solve_noalloc(bilu_plan* P, int nsys, const double* 
       maxl = maxl > P->aiu_rp[i + 1] - P->aiu_rp[i] ? maxl : P->aiu_rp[i + 1] - P->aiu_rp[i];
     }
   e = P->rr ? launch_solve_rr(a, P->rr_lay, P->rr_threads, P->rr_pv, fp32 ? 1 : 0,
-                              o.reduction == BILU_REDUCE_FAST ? 0 : 1, s)
+                              o.reduction == BILU_REDUCE_FAST ? 0 : 1, P->rr_occ4 ? 1 : 0, s)
             : launch_solve(a, P->threads, fp32 ? 1 : 0, o.reduction == BILU_REDUCE_FAST ? 1 : 0, maxl, s);
   if (e != cudaSuccess) return cuda_fail(e, "solver launch");
   return BILU_OK;

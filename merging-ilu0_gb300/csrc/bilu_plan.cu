@@ -391,8 +391,10 @@ void choose_layout(bilu_plan& P) {
 // and the shared-memory staging `mask` (bit 0 A, bit 1 aiL / aiA, bit 2 aiU;
 // operands that would cost occupancy are left in global memory, read through
 // L1; ILU factors are always staged; bit 3: the SpMVs read SELL-32 copies of
-// the operands left in global memory); false when the kernel does not apply or
-// that configuration is invalid.
+// the operands left in global memory; bit 4: the kernel variant with 4 CTAs of
+// 128 threads per SM, taken for 8 rows per thread without ILU factors and
+// otherwise ignored); false when the kernel does not apply or that
+// configuration is invalid.
 bool rr_configure(bilu_plan& P, int nt, int mask) {
   const bilu_options& o = P.opts;
   const int pk = prec_kind(o.precond);
@@ -411,6 +413,7 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
     if (nt != 32 || (pv != 0 && pv != 3) || P.a_maxl > 16) return false;
     mask &= 7;
   }
+  const bool occ4 = (mask & 16) != 0 && R == 8 && pv != 3;
   const bool fp32 = is_fp32(o);
   const int fts = fp32 ? 4 : 8;
   if (pv == 3 && P.tp_lo.empty()) return false;
@@ -426,7 +429,7 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const void* k = rr_kernel(pv, fp32 ? 1 : 0, R, ref ? 1 : 0);
+  const void* k = rr_kernel(pv, fp32 ? 1 : 0, R, ref ? 1 : 0, occ4 ? 1 : 0);
   if (!k) return false;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(optin, off)) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, nt, off) != cudaSuccess || occ < 1) {
@@ -447,6 +450,7 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   P.rr_pv = pv;
   P.rr_lay = L;
   P.rr_sell = (mask & 8) != 0 && !P.sa_off.empty();
+  P.rr_occ4 = occ4;
   return true;
 }
 
@@ -667,7 +671,7 @@ bilu_status check_opts(const bilu_options* o) {
     return set_error(BILU_ERR_INVALID, "options: threads_per_system must be 0..1024");
   if (!(o->parilu_res_tol >= 0.0)) return set_error(BILU_ERR_INVALID, "options: parilu_res_tol must be >= 0");
   if (o->isai_lower_diag != 0 && o->isai_lower_diag != 1) return set_error(BILU_ERR_INVALID, "options: isai_lower_diag");
-  if (o->smem_staging < -1 || o->smem_staging > 15) return set_error(BILU_ERR_INVALID, "options: smem_staging must be -1..15");
+  if (o->smem_staging < -1 || o->smem_staging > 31) return set_error(BILU_ERR_INVALID, "options: smem_staging must be -1..31");
   return BILU_OK;
 }
 
@@ -891,11 +895,12 @@ bilu_status bilu_plan_autotune(bilu_plan* P, int nsys, const double* d_values, c
   const int base = round_up((P->n + 7) / 8, 32);
   const int keep_nt = P->rr_threads;
   const RRLayout keep_lay = P->rr_lay;
-  const bool keep_sell = P->rr_sell;
+  const bool keep_sell = P->rr_sell, keep_occ4 = P->rr_occ4;
   float best = -1.0f;
   int best_nt = keep_nt, best_mask = -1;
   for (int f : {1, 2, 4}) {
-    for (int mask : {0, 2, 6, 1, 8, 10, 14}) {
+    for (int mask : {0, 2, 6, 1, 8, 10, 14, 16, 18, 22, 24, 26}) {
+      if ((mask & 16) && (rr_rows_per_thread(P->n, base * f) != 8 || P->rr_pv == 3)) continue;  // bit 4 ignored
       if (!rr_configure(*P, base * f, mask)) continue;
       float ms = 0.0f;
       for (int rep = 0; rep < 2; ++rep) {  // the first run warms caches; the second is timed
@@ -921,6 +926,7 @@ bilu_status bilu_plan_autotune(bilu_plan* P, int nsys, const double* d_values, c
     P->rr_threads = keep_nt;
     P->rr_lay = keep_lay;
     P->rr_sell = keep_sell;
+    P->rr_occ4 = keep_occ4;
   }
   P->timing = had_timing;
   return st;
@@ -958,7 +964,7 @@ bilu_status bilu_plan_get_info(const bilu_plan* P, bilu_plan_info* info) {
     info->threads = P->rr_threads;
     info->smem_bytes = P->rr_lay.total;
     info->operands_in_smem = (P->rr_lay.A >= 0 ? 1 : 0) | (P->rr_lay.ail >= 0 ? 2 : 0) | (P->rr_lay.aiu >= 0 ? 4 : 0) |
-                             (P->rr_sell ? 8 : 0);
+                             (P->rr_sell ? 8 : 0) | (P->rr_occ4 ? 16 : 0);
   }
   return BILU_OK;
 }
@@ -1125,7 +1131,7 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
     a.A_sell = (const double*)(ws + off_asell);
   }
   e = P->rr ? launch_solve_rr(a, P->rr_lay, P->rr_threads, P->rr_pv, fp32 ? 1 : 0,
-                              o.reduction == BILU_REDUCE_FAST ? 0 : 1, st)
+                              o.reduction == BILU_REDUCE_FAST ? 0 : 1, P->rr_occ4 ? 1 : 0, st)
             : launch_solve(a, P->threads, fp32 ? 1 : 0, o.reduction == BILU_REDUCE_FAST ? 1 : 0, maxl, st);
   if (e != cudaSuccess) return cuda_err(e, "solver launch");
   if (P->timing) cudaEventRecord(P->ev[2], st);

@@ -661,6 +661,24 @@ __global__ void BILU_RR_BOUNDS k_bicgstab_rr(const SolveArgs a, const RRLayout L
                                  a.x + (size_t)sys * P.n);
 }
 
+// The same solver with 4 CTAs of 128 threads per SM: 128 registers per
+// thread instead of 168, at the cost of a few spilled values (tens of bytes
+// per thread, through L1) and a smaller L1 beside the fourth CTA's shared
+// memory.  Measured on GB300: faster when the operands are read through L1
+// and the systems are small (3D 7-point 7x7x7, 2D 24x24 convection-diffusion,
+// no preconditioner), slower with FP64 ISAI values, so the plan's autotuner
+// chooses (staging bit 4).  Not for ILU factors, whose shared-memory layout
+// admits 3 CTAs per SM anyway.
+template <int PV, typename FT>
+__global__ void __launch_bounds__(128, 4) k_bicgstab_rr_occ4(const SolveArgs a, const RRLayout L) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int sys = blockIdx.x;
+  if (sys >= a.nsys) return;
+  const DevPattern& P = a.pat;
+  rr_solve<8, PV, FT, true, false>(a, P, L, smem, sys, a.A + (size_t)sys * P.a_nnz, a.b + (size_t)sys * P.n,
+                                   a.x + (size_t)sys * P.n);
+}
+
 // one CTA per system of an uneven-batch bucket (own size and pattern each):
 // CTA b solves system order[b] (longest first), merged ILU(0) (PV 3) or none
 // (PV 0), no optional staging
@@ -743,7 +761,13 @@ int rr_rows_per_thread(int n, int nt) {
 
 int rr_max_threads(int R) { return R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 : 128)); }
 
-const void* rr_kernel(int pv, int fp32, int R, int ref) {
+const void* rr_kernel(int pv, int fp32, int R, int ref, int occ4) {
+  if (occ4) {  // FAST order, 8 rows per thread, ISAI or no preconditioner
+    if (ref || R != 8 || pv == 3) return nullptr;
+    if (pv == 0) return (const void*)k_bicgstab_rr_occ4<0, double>;
+    if (pv == 1) return fp32 ? (const void*)k_bicgstab_rr_occ4<1, float> : (const void*)k_bicgstab_rr_occ4<1, double>;
+    return fp32 ? (const void*)k_bicgstab_rr_occ4<2, float> : (const void*)k_bicgstab_rr_occ4<2, double>;
+  }
   if (ref) {  // reference order: no preconditioner or ILU factors (one warp per system)
     if (pv == 0) return rr_kernel_pv<0, double, true>(R);
     if (pv == 3) return fp32 ? rr_kernel_pv<3, float, true>(R) : rr_kernel_pv<3, double, true>(R);
@@ -755,12 +779,12 @@ const void* rr_kernel(int pv, int fp32, int R, int ref) {
   return fp32 ? rr_kernel_pv<2, float, false>(R) : rr_kernel_pv<2, double, false>(R);
 }
 
-cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, int ref,
+cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, int ref, int occ4,
                             cudaStream_t st) {
   if (a.nsys == 0) return cudaSuccess;
   const int R = rr_rows_per_thread(a.pat.n, nt);
   if (R == 0 || nt % 32 || nt > rr_max_threads(R) || (ref && nt != 32)) return cudaErrorInvalidConfiguration;
-  const void* k = rr_kernel(pv, fp32, R, ref);
+  const void* k = rr_kernel(pv, fp32, R, ref, occ4);
   if (!k) return cudaErrorInvalidConfiguration;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total);
   if (e != cudaSuccess) return e;

@@ -216,7 +216,7 @@ def test_rr_lu_edge_cases(cuda):
                                             ("cd2d_12x12", bilu.PRECOND_ILU0, dict(ilu_approach=1)),
                                             ("3d7_5x5x5", bilu.PRECOND_GENERAL_ISAI, dict(isai_power=2))],
                          ids=["parilu_isai", "merged_ilu0", "general_isai"])
-@pytest.mark.parametrize("staging", [0, 8, 9, 14])
+@pytest.mark.parametrize("staging", [0, 8, 9, 14, 16, 26])
 @pytest.mark.parametrize("fp32", [False, True])
 def test_rr_operand_layouts_bitwise(cuda, fam, precond, kw, staging, fp32):
     """Shared-memory staging and the SELL-32 copies of A and aiU change where the SpMVs read their operands,
