@@ -60,7 +60,8 @@ SECONDARY = [
          desc="16384 2D 5-point 16x16 systems, merged ILU(0) with FP32-stored factors, FAST order",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1)),
     dict(name="plain_ilu0_2d5_16x16_ref", kind=1, grid=(16, 16, 1), nsys=16384,
-         desc="plain form in the reference's operation order (bit-identical iterates; shared-memory kernel)",
+         desc="plain form in the reference's operation order (bit-identical iterates; register-resident one-warp "
+              "kernel)",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=0)),
     dict(name="fp32_isai_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768, autotune=True,
          desc="ILU(0) + ISAI stored and applied in FP32 (FP64 A*x, inner products, recurrences), 32768 "
@@ -455,6 +456,9 @@ def main():
     ap.add_argument("--nsys", type=int, default=0, help="override the headline batch size (profiling runs)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the plan's default solver configuration (profiling runs: fixed launch sequence)")
+    ap.add_argument("--smem-staging", type=int, default=-1,
+                    help="with --no-autotune: the solver configuration mask (bilu_options.smem_staging), e.g. the "
+                         "one the autotuner chooses, so that a profiling run launches that kernel")
     ap.add_argument("--workload", default="",
                     help="with --kernel-only: measure this secondary workload (by name) instead of the headline "
                          "(profiling runs)")
@@ -467,6 +471,10 @@ def main():
         HEADLINE.update(found[0])
     if args.no_autotune:
         HEADLINE["autotune"] = False
+    if args.smem_staging >= 0:
+        if not args.no_autotune:
+            ap.error("--smem-staging needs --no-autotune")
+        HEADLINE["opts"] = dict(HEADLINE["opts"], smem_staging=args.smem_staging)
     if args.nsys > 0:
         HEADLINE["desc"] = HEADLINE["desc"].replace(f"{HEADLINE['nsys']} FP64", f"{args.nsys} FP64")
         HEADLINE["nsys"] = args.nsys
