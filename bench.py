@@ -77,9 +77,10 @@ SECONDARY = [
 
 
 # DRAM bytes (read + write) of one register-resident solver launch on the headline workload, per
-# system: ncu dram__bytes_read.sum + dram__bytes_write.sum of a 3072-system launch (413.8 MB) / 3072;
-# the traffic grows in proportion to the systems of a launch.
-RR_TRAFFIC_BYTES_PER_SYSTEM = 134_689
+# system, in the configuration the autotuner chooses there (the 4-CTA-per-SM variant, operands read
+# through L1: smem_staging 16): ncu dram__bytes_read.sum + dram__bytes_write.sum of a 3072-system
+# launch (430.4 + 38.0 MB) / 3072; the traffic grows in proportion to the systems of a launch.
+RR_TRAFFIC_BYTES_PER_SYSTEM = 152_460
 
 
 def bytes_per_system(n, nnz):
@@ -602,7 +603,9 @@ def main():
         "gpu_launches": launches_per_step(info) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": RR_TRAFFIC_BYTES_PER_SYSTEM * nsys if info["solver_kernel"] == 1 and fp32_prec
-                     else None, "traffic_source": "ncu capture of 3072 systems, scaled per system", "peak_kind": peak_kind, "kernel": "k_bicgstab_rr (register-resident solver)" if info["solver_kernel"] == 1 else "k_bicgstab (solver)",
+                     else None, "traffic_source": "ncu capture of 3072 systems, scaled per system", "peak_kind": peak_kind, "kernel": ("k_bicgstab_rr_occ4 (register-resident solver, 4 CTAs per SM)" if info["operands_in_smem"] & 16
+                                else "k_bicgstab_rr (register-resident solver)") if info["solver_kernel"] == 1
+                     else "k_bicgstab (solver)",
                      "bytes_per_system": bps},
         "roofline_fp64": {"achieved": flops / solve_s / 1e9, "peak": fp64_peak, "unit": "GFLOP/s",
                           "frac": flops / solve_s / 1e9 / fp64_peak,
