@@ -167,7 +167,7 @@ typedef struct bilu_plan_info {
                             4-CTAs-per-SM variant of the register-resident kernel */
   int solver_kernel;     /* 0: one CTA per system, vectors in shared memory (every mode);
                             1: register-resident (BILU_REDUCE_FAST with n <= 1024, or
-                            the reference order with n <= 256, ILU factors or none and
+                            the reference order with n <= 1024, ILU factors or none and
                             rows of at most 16 entries): `threads` threads per system,
                             each owning rows t + k * threads                         */
 } bilu_plan_info;

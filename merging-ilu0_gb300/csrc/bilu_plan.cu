@@ -405,12 +405,12 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   if (R == 0 || nt > rr_max_threads(R)) return false;
   const bool lu = (pk == PK_ILU_INKERNEL || pk == PK_LU_GLOBAL);
   const int pv = pk == PK_NONE ? 0 : (lu ? 3 : (P.general_isai ? 2 : 1));
-  // Reference order: one warp per system, whose inner products are the
+  // Reference order: the inner products chain through the warps as the
   // reference's warp-0 sums; ILU factors or none (the ISAI solvers' serial
   // inner products stay on the shared-memory kernel), rows of at most 16
-  // entries (row_ref<16>), no SELL-32 copies.
+  // entries (row_ref<16>), no SELL-32 copies, no 4-CTA variant.
   if (ref) {
-    if (nt != 32 || (pv != 0 && pv != 3) || P.a_maxl > 16) return false;
+    if ((pv != 0 && pv != 3) || P.a_maxl > 16) return false;
     mask &= 7;
   }
   const bool occ4 = (mask & 16) != 0 && R == 8 && pv != 3;
@@ -466,7 +466,6 @@ void choose_rr(bilu_plan& P) {
   const bilu_options& o = P.opts;
   P.rr = false;
   int nt = o.threads_per_system > 0 ? o.threads_per_system : round_up((P.n + 7) / 8, 32);
-  if (o.reduction != BILU_REDUCE_FAST && o.threads_per_system <= 0) nt = 32;  // reference order: one warp
   const bool lu = prec_kind(o.precond) == PK_ILU_INKERNEL || prec_kind(o.precond) == PK_LU_GLOBAL;
   rr_configure(P, nt, o.smem_staging >= 0 ? o.smem_staging : (6 | (lu && P.n > 512 ? 8 : 0)));
 }
@@ -901,6 +900,7 @@ bilu_status bilu_plan_autotune(bilu_plan* P, int nsys, const double* d_values, c
   for (int f : {1, 2, 4}) {
     for (int mask : {0, 2, 6, 1, 8, 10, 14, 16, 18, 22, 24, 26}) {
       if ((mask & 16) && (rr_rows_per_thread(P->n, base * f) != 8 || P->rr_pv == 3)) continue;  // bit 4 ignored
+      if ((mask & 24) && P->opts.reduction != BILU_REDUCE_FAST) continue;                         // bits 3, 4 ignored
       if (!rr_configure(*P, base * f, mask)) continue;
       float ms = 0.0f;
       for (int rep = 0; rep < 2; ++rep) {  // the first run warms caches; the second is timed

@@ -1,9 +1,8 @@
 // Register-resident batched BiCGSTAB for BILU_REDUCE_FAST with an ISAI
 // preconditioner (two triangles or the general ISAI of A), in-place ILU
-// factors (factorised in the kernel, the merged form, or given) or none; and,
-// for n <= 256, ILU factors or none in the reference's operation order (REF:
-// one warp per system; the variant's comment at k_bicgstab_rr says why that
-// order is the reference's).
+// factors (factorised in the kernel, the merged form, or given) or none; and
+// ILU factors or none in the reference's operation order (REF: rows of at
+// most 16 entries; ref_chain_sum says why the order is the reference's).
 //
 // Same method, exits and iteration counting as the shared-memory kernel
 // (k_solve.cu, after PrecondBiCGSTAB_exact_ilu0_app1_merged_gpu.cu:249-538,
@@ -105,6 +104,40 @@ __device__ __forceinline__ bool block_sum_w0(double (&v)[K], double* red, int nw
       for (int w = 1; w < nw; ++w) s = s + red[k * nt + w];
       v[k] = s;
     }
+  }
+  return true;
+}
+
+// Reference order with W = nw warps.  The reference sums an inner product on
+// one warp: lane l runs fma over rows l, l+32, l+64, ... in order from 0.0,
+// then a shfl_down tree (Bicgstab_common.hpp:195-250).  Warp w owns lane l's
+// rows l + 32 (w R + k), k < R, the w-th block of that sequence, so the chain
+// passes from warp to warp through red (one barrier per warp).  The last warp
+// then runs the xor butterfly: its lane 0 adds the same pairs as the shfl_down
+// tree (IEEE addition commutes).  term(k, acc) adds row k's terms to the K
+// accumulators (nothing for rows >= n).  Returns true on the last warp, which
+// forms the scalar recurrence and broadcasts it.  One warp: no barrier.
+template <int K, int R, typename Term>
+__device__ __forceinline__ bool ref_chain_sum(double (&v)[K], Term term, double* red, int nw) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int w = 0; w < nw; ++w) {
+    if (warp == w) {
+#pragma unroll
+      for (int j = 0; j < K; ++j) v[j] = w == 0 ? 0.0 : red[j * 32 + lane];
+#pragma unroll
+      for (int k = 0; k < R; ++k) term(k, v);
+      if (w + 1 < nw) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) red[j * 32 + lane] = v[j];
+      }
+    }
+    if (w + 1 < nw) __syncthreads();
+  }
+  if (warp != nw - 1) return false;
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v[j] = v[j] + __shfl_xor_sync(kFull, v[j], off);
   }
   return true;
 }
@@ -301,6 +334,11 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
                                          unsigned char* smem, const int sys, const double* Ag, const double* bg,
                                          double* xg) {
   const int n = P.n, nt = blockDim.x, tid = threadIdx.x, nw = nt >> 5;
+  // this thread's rows: rb + k * rs, k < R.  FAST: tid + k * nt.  REF: lane +
+  // 32 (warp R + k), so that a warp's rows are a block of the reference's
+  // lane-strided inner-product terms (ref_chain_sum)
+  const int rb = REF ? (tid & 31) + 32 * R * (tid >> 5) : tid;
+  const int rs = REF ? 32 : nt;
   const int* __restrict__ arp = P.a_rp;
   const auto* __restrict__ aci = pick_ci<C16>(P.a_ci16, P.a_ci);
   const auto* __restrict__ lci = pick_ci<C16>(P.ail_ci16, P.ail_ci);
@@ -400,7 +438,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
   double q[1] = {0.0};
 #pragma unroll
   for (int k = 0; k < R; ++k) {
-    const int i = tid + k * nt;
+    const int i = rb + k * rs;
     const double bi = i < n ? __ldg(bg + i) : 0.0;
     x[k] = 0.0;
     p[k] = 0.0;
@@ -413,7 +451,15 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
   // also completes the staging above).  bc: the scalars warp 0 broadcasts.
   double* bc = red + 2 * nt;
   const bool lane0 = (tid & 31) == 0;
-  if (block_sum_w0<1, PV != 3>(q, red, nw) && lane0) {
+  // the CTA's sum of q (and of its second slot for K = 2): FAST, the block
+  // reduction of the thread partials; REF, the reference's chain over the
+  // rows, term(k, acc) per row
+#define BILU_RR_SUM(K, qv, TERM) \
+  (REF ? ref_chain_sum<K, R>(qv, TERM, red, nw) : block_sum_w0<K, PV != 3>(qv, red, nw))
+  auto t_bb = [&](int k, double(&acc)[1]) {
+    if (rb + k * rs < n) acc[0] = fma(r[k], r[k], acc[0]);
+  };
+  if (BILU_RR_SUM(1, q, t_bb) && lane0) {
     bc[0] = sqrt(q[0]);
     bc[1] = q[0];
   }
@@ -441,26 +487,26 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
   do {                                                                                                           \
     if (PV == 1) {                                                                                               \
       FT z_[R];                                                                                                  \
-      rows_acc<R>(AIL, lci, P.ail_rp, tid, nt, n, sin, z_);                                                 \
+      rows_acc<R>(AIL, lci, P.ail_rp, rb, rs, n, sin, z_);                                                 \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
-        const int i = tid + k * nt;                                                                              \
+        const int i = rb + k * rs;                                                                              \
         if (i < n) smid[i] = z_[k];                                                                              \
       }                                                                                                          \
       __syncthreads();                                                                                           \
       if (AIUsell)                                                                                               \
-        rows_acc_sell<R>(AIUsell, suci, P.su_off, P.aiu_rp, tid, nt, n, smid, z_);                            \
+        rows_acc_sell<R>(AIUsell, suci, P.su_off, P.aiu_rp, rb, rs, n, smid, z_);                            \
       else                                                                                                       \
-        rows_acc<R>(AIU, uci, P.aiu_rp, tid, nt, n, smid, z_);                                              \
+        rows_acc<R>(AIU, uci, P.aiu_rp, rb, rs, n, smid, z_);                                              \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
-        const int i = tid + k * nt;                                                                              \
+        const int i = rb + k * rs;                                                                              \
         if (i < n) sph[i] = (double)z_[k];                                                                       \
       }                                                                                                          \
       __syncthreads();                                                                                           \
     } else if (PV == 2) {                                                                                        \
       FT z_[R];                                                                                                  \
-      rows_acc<R>(AIL, lci, P.ail_rp, tid, nt, n, sin, z_);                                                 \
+      rows_acc<R>(AIL, lci, P.ail_rp, rb, rs, n, sin, z_);                                                 \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
-        const int i = tid + k * nt;                                                                              \
+        const int i = rb + k * rs;                                                                              \
         if (i < n) sph[i] = (double)z_[k];                                                                       \
       }                                                                                                          \
       __syncthreads();                                                                                           \
@@ -472,7 +518,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
 #define BILU_RR_INPUT(vec)                       \
   do {                                           \
     _Pragma("unroll") for (int k = 0; k < R; ++k) { \
-      const int i = tid + k * nt;                \
+      const int i = rb + k * rs;                \
       if (i < n) {                               \
         if (PV == 0 || (PV == 3 && sizeof(FT) == 8)) \
           sph[i] = vec[k];                       \
@@ -495,18 +541,21 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     BILU_RR_APPLY();  // p_hat in sph
     // v = A p_hat, (r_hat, v)
     if (REF)
-      rows_acc_ref<R>(Am, aci, arp, tid, nt, n, sph, v);
+      rows_acc_ref<R>(Am, aci, arp, rb, rs, n, sph, v);
     else if (Asell)
-      rows_acc_sell<R>(Asell, saci, P.sa_off, arp, tid, nt, n, sph, v);
+      rows_acc_sell<R>(Asell, saci, P.sa_off, arp, rb, rs, n, sph, v);
     else
-      rows_acc<R>(Am, aci, arp, tid, nt, n, sph, v);
+      rows_acc<R>(Am, aci, arp, rb, rs, n, sph, v);
     q[0] = 0.0;
+    auto t_bv = [&](int k, double(&acc)[1]) {
+      const int i = rb + k * rs;
+      if (i < n) acc[0] = fma(__ldg(bg + i), v[k], acc[0]);
+    };
+    if (!REF) {
 #pragma unroll
-    for (int k = 0; k < R; ++k) {
-      const int i = tid + k * nt;
-      if (i < n) q[0] = fma(__ldg(bg + i), v[k], q[0]);
+      for (int k = 0; k < R; ++k) t_bv(k, q);
     }
-    if (block_sum_w0<1, PV != 3>(q, red, nw) && lane0) bc[2] = rho / q[0];
+    if (BILU_RR_SUM(1, q, t_bv) && lane0) bc[2] = rho / q[0];
     __syncthreads();
     alpha = bc[2];
     // x += alpha p_hat, s = r - alpha v, ||s||.  p_hat is read before anyone
@@ -515,15 +564,15 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     q[0] = 0.0;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-      const int i = tid + k * nt;
+      const int i = rb + k * rs;
       if (i < n) {
         x[k] = fma(alpha, sph[i], x[k]);
         r[k] = fma(-alpha, v[k], r[k]);
-        q[0] = fma(r[k], r[k], q[0]);
+        if (!REF) q[0] = fma(r[k], r[k], q[0]);
       }
     }
     BILU_RR_INPUT(r);
-    if (block_sum_w0<1, PV != 3>(q, red, nw) && lane0) bc[3] = sqrt(q[0]);
+    if (BILU_RR_SUM(1, q, t_bb) && lane0) bc[3] = sqrt(q[0]);
     __syncthreads();
     res = bc[3];
     iter = iter + 0.5f;
@@ -534,37 +583,45 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     BILU_RR_APPLY();  // s_hat in sph
     // t = A s_hat, (t, s), (t, t)
     if (REF)
-      rows_acc_ref<R>(Am, aci, arp, tid, nt, n, sph, t);
+      rows_acc_ref<R>(Am, aci, arp, rb, rs, n, sph, t);
     else if (Asell)
-      rows_acc_sell<R>(Asell, saci, P.sa_off, arp, tid, nt, n, sph, t);
+      rows_acc_sell<R>(Asell, saci, P.sa_off, arp, rb, rs, n, sph, t);
     else
-      rows_acc<R>(Am, aci, arp, tid, nt, n, sph, t);
+      rows_acc<R>(Am, aci, arp, rb, rs, n, sph, t);
     double q2[2] = {0.0, 0.0};
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      const int i = tid + k * nt;
-      if (i < n) {
-        q2[0] = fma(t[k], r[k], q2[0]);
-        q2[1] = fma(t[k], t[k], q2[1]);
+    auto t_ts = [&](int k, double(&acc)[2]) {
+      if (rb + k * rs < n) {
+        acc[0] = fma(t[k], r[k], acc[0]);
+        acc[1] = fma(t[k], t[k], acc[1]);
       }
+    };
+    if (!REF) {
+#pragma unroll
+      for (int k = 0; k < R; ++k) t_ts(k, q2);
     }
-    if (block_sum_w0<2, PV != 3>(q2, red, nw) && lane0) bc[4] = q2[0] / q2[1];
+    if (BILU_RR_SUM(2, q2, t_ts) && lane0) bc[4] = q2[0] / q2[1];
     __syncthreads();
     const double omega = bc[4];
     // x += omega s_hat, r = s - omega t, ||r||, next rho = (r, r_hat)
     q2[0] = 0.0;
     q2[1] = 0.0;
+    auto t_rr = [&](int k, double(&acc)[2]) {
+      const int i = rb + k * rs;
+      if (i < n) {
+        acc[0] = fma(r[k], r[k], acc[0]);
+        acc[1] = fma(__ldg(bg + i), r[k], acc[1]);
+      }
+    };
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-      const int i = tid + k * nt;
+      const int i = rb + k * rs;
       if (i < n) {
         x[k] = fma(omega, sph[i], x[k]);
         r[k] = fma(-omega, t[k], r[k]);
-        q2[0] = fma(r[k], r[k], q2[0]);
-        q2[1] = fma(__ldg(bg + i), r[k], q2[1]);
       }
+      if (!REF) t_rr(k, q2);
     }
-    if (block_sum_w0<2, PV != 3>(q2, red, nw) && lane0) {
+    if (BILU_RR_SUM(2, q2, t_rr) && lane0) {
       bc[5] = sqrt(q2[0]);
       bc[6] = q2[1];
       bc[7] = (q2[1] / rho) * (alpha / omega);  // the next iteration's beta: (rho_new / rho_old) * (alpha / omega_old)
@@ -581,12 +638,13 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     }
   }
 #undef BILU_RR_APPLY
+#undef BILU_RR_SUM
 #undef BILU_RR_INPUT
 
   // ---- write back
 #pragma unroll
   for (int k = 0; k < R; ++k) {
-    const int i = tid + k * nt;
+    const int i = rb + k * rs;
     if (i < n) xg[i] = x[k];
   }
   if (tid == 0) {
@@ -603,37 +661,46 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
     __syncthreads();  // every reader of sph is done
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-      const int i = tid + k * nt;
+      const int i = rb + k * rs;
       if (i < n) sph[i] = x[k];
     }
     __syncthreads();
     double ax[R];
     if (REF) {
       // KernelFillTrueResNorms (Bicgstab_common.hpp:294-342): row_ref sums, then one serial
-      // inner product over i = 0 .. n-1 -- the single warp passes each row's residual to every
-      // lane in row order, and every lane runs the same FMA chain
-      rows_acc_ref<R>(Am, aci, arp, tid, nt, n, sph, ax);
+      // inner product over i = 0 .. n-1.  Warp w holds rows 32 (w R + k) + l: it passes each
+      // row's residual to every lane in row order, every lane runs the same FMA chain, and the
+      // chain moves on to the next warp through red
+      rows_acc_ref<R>(Am, aci, arp, rb, rs, n, sph, ax);
+      const int lane = tid & 31, warp = tid >> 5;
       double acc = 0.0;
+      for (int w = 0; w < nw; ++w) {
+        if (warp == w) {
+          if (w > 0) acc = red[0];
 #pragma unroll
-      for (int k = 0; k < R; ++k) {
-        const int i0 = tid + k * nt;
-        const double ri = i0 < n ? __ldg(bg + i0) - ax[k] : 0.0;
-        for (int l = 0; l < 32; ++l) {
-          const double rl = __shfl_sync(kFull, ri, l);
-          if (k * 32 + l < n) acc = fma(rl, rl, acc);
+          for (int k = 0; k < R; ++k) {
+            const int i0 = rb + k * rs;
+            const double ri = i0 < n ? __ldg(bg + i0) - ax[k] : 0.0;
+            for (int l = 0; l < 32; ++l) {
+              const double rl = __shfl_sync(kFull, ri, l);
+              if (32 * (w * R + k) + l < n) acc = fma(rl, rl, acc);
+            }
+          }
+          if (w + 1 < nw && lane == 0) red[0] = acc;
         }
+        if (w + 1 < nw) __syncthreads();
       }
-      if (tid == 0) a.true_res[sys] = sqrt(acc);
+      if (warp == nw - 1 && lane == 0) a.true_res[sys] = sqrt(acc);
       return;
     }
     if (Asell)
-      rows_acc_sell<R>(Asell, saci, P.sa_off, arp, tid, nt, n, sph, ax);
+      rows_acc_sell<R>(Asell, saci, P.sa_off, arp, rb, rs, n, sph, ax);
     else
-      rows_acc<R>(Am, aci, arp, tid, nt, n, sph, ax);
+      rows_acc<R>(Am, aci, arp, rb, rs, n, sph, ax);
     q[0] = 0.0;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-      const int i = tid + k * nt;
+      const int i = rb + k * rs;
       if (i < n) {
         const double ri = __ldg(bg + i) - ax[k];
         q[0] = fma(ri, ri, q[0]);
@@ -646,11 +713,10 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
 #define BILU_RR_BOUNDS __launch_bounds__(R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 : 128)), R == 8 ? 3 : 1)
 
 // one CTA per system of a batch sharing one pattern
-// REF: the reference's operation order, one warp per system (n <= 256; the
-// plan checks): thread l's rows l, l+32, ... are the reference's lane-strided
-// inner-product terms, and lane 0 of the xor butterfly adds the same pairs as
-// its shfl_down tree (IEEE addition commutes), so every scalar is the
-// reference's bit for bit.
+// REF: the reference's operation order.  Warp w's lane l owns rows
+// l + 32 (w R + k), a block of the reference's lane-strided inner-product
+// terms; the inner products chain through the warps in order (ref_chain_sum),
+// so every scalar is the reference's bit for bit.
 template <int R, int PV, typename FT, bool REF = false>
 __global__ void BILU_RR_BOUNDS k_bicgstab_rr(const SolveArgs a, const RRLayout L) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -783,7 +849,7 @@ cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int p
                             cudaStream_t st) {
   if (a.nsys == 0) return cudaSuccess;
   const int R = rr_rows_per_thread(a.pat.n, nt);
-  if (R == 0 || nt % 32 || nt > rr_max_threads(R) || (ref && nt != 32)) return cudaErrorInvalidConfiguration;
+  if (R == 0 || nt % 32 || nt > rr_max_threads(R)) return cudaErrorInvalidConfiguration;
   const void* k = rr_kernel(pv, fp32, R, ref, occ4);
   if (!k) return cudaErrorInvalidConfiguration;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total);

@@ -15,6 +15,8 @@ FAMILIES = {
     "3d7_5x5x5": (2, 5, 5, 5),
     "cd2d_12x12": (4, 12, 12, 1),
     "3d7_7x7x7": (5, 7, 7, 7),
+    "cd2d_24x24": (4, 24, 24, 1),
+    "3d7_10x10x10": (2, 10, 10, 10),
 }
 
 

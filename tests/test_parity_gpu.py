@@ -103,6 +103,28 @@ def test_unpreconditioned_bitwise(cuda, precond):
     _compare(g, o, "no preconditioner")
 
 
+@pytest.mark.parametrize("family,threads", [("3d7_7x7x7", 0), ("3d7_7x7x7", 128), ("3d7_7x7x7", 256),
+                                            ("cd2d_24x24", 0), ("3d7_10x10x10", 0)],
+                         ids=["7x7x7-2warps", "7x7x7-4warps", "7x7x7-8warps", "24x24-3warps", "10x10x10-4warps"])
+@pytest.mark.parametrize("precond,fp32", [(bilu.PRECOND_ILU0, False), (bilu.PRECOND_ILU0, True),
+                                          (bilu.PRECOND_NONE, False)], ids=["ilu0", "ilu0-fp32", "none"])
+def test_reference_order_several_warps_bitwise(cuda, family, threads, precond, fp32):
+    """The register-resident kernel in the reference order with several warps per system: each inner
+    product chains through the warps (warp w holds a block of every lane's rows), so it equals the
+    reference's warp-0 sum, and the true residual its serial sum, bit for bit."""
+    nsys = 8
+    rp, ci, v, b = H.workload(family, nsys)
+    kw = dict(tol_mode=1, tol=1e-10) if fp32 else {}
+    o = H.oracle_pipeline(rp, ci, v, b, precond, fp32=fp32, **kw)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, threads_per_system=threads,
+                    factor_precision=bilu.FP32 if fp32 else bilu.FP64, **kw)
+    assert g["info"]["solver_kernel"] == 1
+    if threads:
+        assert g["info"]["threads"] == threads
+    _compare(g, o, f"reference order {family} threads {g['info']['threads']} precond {precond} fp32={fp32}")
+    assert np.all(g["conv"] == 1)
+
+
 def test_relative_tolerance_bitwise(cuda):
     rp, ci, v, b = H.workload("2d5_16x16", NSYS)
     o = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_ILU0, tol_mode=1, tol=1e-10)
