@@ -292,24 +292,29 @@ bilu_status bilu_true_residual(const bilu_plan* plan, int nsys, const double* d_
  * starting at 0), columns nnz_s per system; device values / b / x are the
  * concatenation of the systems' arrays in the same order (value offset of
  * system s = sum of the earlier sys_nnz, vector offset = sum of the earlier sys_n).
- * The plan sorts the systems into size buckets (n <= 128, 256, 512, 1024,
- * larger); each bucket runs as one persistent kernel over a work queue
- * (largest systems first), and a solve replays one CUDA graph holding every
- * bucket launch on concurrent branches.  The graph is captured on the first
- * solve and again whenever the device pointers change. */
+ * The plan sorts the systems into size buckets, in the reference order
+ * n <= 128, 256, 512, 1024, larger (5 buckets), each run as one persistent
+ * kernel over a work queue (largest systems first); in BILU_REDUCE_FAST order
+ * n <= 64, 96, 128, 192, 256, 384, 512, 768, 1024, larger (10 buckets), those
+ * with n <= 1024 run as one register-resident CTA per system (largest first).
+ * A solve replays one CUDA graph holding every bucket launch on concurrent
+ * branches.  The graph is captured on the first solve and again whenever the
+ * device pointers change. */
 typedef struct bilu_uneven_plan bilu_uneven_plan;
 bilu_status bilu_uneven_plan_create(bilu_uneven_plan** plan, int nsys, const int* h_sys_n, const int* h_sys_nnz,
                                     const int* h_row_ptrs, const int* h_col_idxs, const bilu_options* opts);
 bilu_status bilu_uneven_plan_destroy(bilu_uneven_plan* plan);
-/* Times every candidate CTA size (64..1024 threads, persistent grid from the
- * occupancy of each) per bucket on the given batch and keeps the fastest.
+/* Times every candidate CTA size per bucket on the given batch and keeps the
+ * fastest: 64..1024 threads with the persistent grid from the occupancy of
+ * each, or, for register-resident buckets, 1x, 2x and 4x the fewest threads.
  * Synchronises the stream; overwrites d_x. */
 bilu_status bilu_uneven_autotune(bilu_uneven_plan* plan, const double* d_values, const double* d_b, double* d_x,
                                  void* stream);
 bilu_status bilu_uneven_solve(bilu_uneven_plan* plan, const double* d_values, const double* d_b, double* d_x,
                               const bilu_results* results, void* stream);
-/* Bucket `bucket` (0..4): n range (n_lo, n_hi], systems, chosen CTA size,
- * persistent grid, shared memory per CTA, autotuned time (ms, -1 if not tuned). */
+/* Bucket `bucket` (0 .. count - 1; BILU_ERR_INVALID past the last one): n
+ * range (n_lo, n_hi], systems, chosen CTA size, grid, shared memory per CTA,
+ * autotuned time (ms, -1 if not tuned). */
 bilu_status bilu_uneven_get_info(const bilu_uneven_plan* plan, int bucket, int* n_lo, int* n_hi, int* systems,
                                  int* threads, int* grid, int* smem_bytes, float* tuned_ms);
 

@@ -239,14 +239,17 @@ class UnevenPlan:
         _check(lib().bilu_uneven_solve(self.h, _dev(values), _dev(b), _dev(x), C.byref(R), _stream(stream)))
 
     def info(self):
+        """Per size bucket: n range, systems, CTA size, grid, shared memory, autotuned time."""
         out = []
-        for k in range(5):
+        while True:
             v = [C.c_int() for _ in range(6)]
             t = C.c_float()
-            _check(lib().bilu_uneven_get_info(self.h, k, *[C.byref(q) for q in v], C.byref(t)))
+            rc = lib().bilu_uneven_get_info(self.h, len(out), *[C.byref(q) for q in v], C.byref(t))
+            if rc == ERR_INVALID and out:
+                return out  # past the last bucket
+            _check(rc)
             out.append(dict(n_lo=v[0].value, n_hi=v[1].value, systems=v[2].value, threads=v[3].value,
                             grid=v[4].value, smem_bytes=v[5].value, tuned_ms=t.value))
-        return out
 
 
 # ---------------------------------------------------------------- plans

@@ -339,12 +339,15 @@ bilu_status bilu_uneven_plan_create(bilu_uneven_plan** out, int nsys, const int*
     delete U;
     return set_error(BILU_ERR_CAPACITY, "uneven batch metadata exceeds 2^31 entries");
   }
-  // size buckets (n in (lo, hi])
-  const int edges[] = {0, 128, 256, 512, 1024, 1 << 30};
+  // size buckets (n in (lo, hi]).  FAST order: edges a factor of about sqrt(2)
+  // apart, because a register-resident bucket launches every system with the
+  // threads and shared memory of its largest one
   const bool fp32 = o.factor_precision == BILU_FP32;
   const bool fast = o.reduction == BILU_REDUCE_FAST;
+  const std::vector<int> edges = fast ? std::vector<int>{0, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1 << 30}
+                                      : std::vector<int>{0, 128, 256, 512, 1024, 1 << 30};
   const int budget = (int)solve_max_smem();
-  for (int e = 0; e + 1 < (int)(sizeof(edges) / sizeof(edges[0])); ++e) {
+  for (size_t e = 0; e + 1 < edges.size(); ++e) {
     Bucket b;
     b.lo = edges[e];
     b.hi = edges[e + 1];
