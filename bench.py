@@ -59,6 +59,10 @@ SECONDARY = [
     dict(name="fp32_ilu0_2d5_16x16", kind=1, grid=(16, 16, 1), nsys=16384,
          desc="16384 2D 5-point 16x16 systems, merged ILU(0) with FP32-stored factors, FAST order",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1)),
+    dict(name="fp32_isai_2d5_16x16", kind=1, grid=(16, 16, 1), nsys=16384, autotune=True,
+         desc="16384 2D 5-point 16x16 systems, ILU(0) + ISAI stored and applied in FP32 (FP64 A*x, inner products, "
+              "recurrences), FAST order",
+         opts=dict(precond=3, ilu_approach=3, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1)),
     dict(name="plain_ilu0_2d5_16x16_ref", kind=1, grid=(16, 16, 1), nsys=16384,
          desc="plain form in the reference's operation order (bit-identical iterates; register-resident one-warp "
               "kernel)",
@@ -565,6 +569,18 @@ def main():
             "workload": "16384 2D 5-point 16x16 systems", "plain_form": "merged FP64 ILU(0) + BiCGSTAB",
             "plain_systems_per_s": p16["systems_per_s"], "chosen_form": "merged ILU(0), FP32-stored factors",
             "chosen_systems_per_s": f16["systems_per_s"], "ratio": f16["systems_per_s"] / p16["systems_per_s"]}
+    i16 = by_name.get("fp32_isai_2d5_16x16")
+    if p16 and i16:
+        chosen["fp32_isai_2d5_16x16"] = {
+            "workload": "16384 2D 5-point 16x16 systems", "plain_form": "merged FP64 ILU(0) + BiCGSTAB",
+            "plain_systems_per_s": p16["systems_per_s"], "chosen_form": "ILU(0) + ISAI stored and applied in FP32",
+            "chosen_systems_per_s": i16["systems_per_s"], "ratio": i16["systems_per_s"] / p16["systems_per_s"]}
+    p24, i24 = by_name.get("fp64_ilu0_cd2d_24x24"), by_name.get("fp32_isai_cd2d_24x24")
+    if p24 and i24:
+        chosen["fp32_isai_cd2d_24x24"] = {
+            "workload": "32768 convection-diffusion systems 24x24", "plain_form": "merged FP64 ILU(0) + BiCGSTAB",
+            "plain_systems_per_s": p24["systems_per_s"], "chosen_form": "ILU(0) + ISAI stored and applied in FP32",
+            "chosen_systems_per_s": i24["systems_per_s"], "ratio": i24["systems_per_s"] / p24["systems_per_s"]}
     for sc in secondary:
         if sc.get("name") == "learned_warm_start_3d7_7x7x7" and "learned" in sc:
             chosen["learned_3d7_7x7x7"] = {
