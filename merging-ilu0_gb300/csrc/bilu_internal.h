@@ -64,10 +64,10 @@ struct DevPattern {
   const int* aiu_ci = nullptr;
   // program per ISAI row: blocks {t, k} followed by k entries {c, pos}; rows
   // in blocks of 32, word j of row 32b+l at prog[prog_ptr[b] + 32j + l]
-  const int* ail_prog_ptr = nullptr;  // (n+31)/32 + 1 block offsets (int2 units)
-  const int2* ail_prog = nullptr;
+  const int* ail_prog_ptr = nullptr;  // (n+31)/32 + 1 block offsets (words)
+  const int* ail_prog = nullptr;      // words t | count << 5 and c | pos << 5 (build_isai)
   const int* aiu_prog_ptr = nullptr;
-  const int2* aiu_prog = nullptr;
+  const int* aiu_prog = nullptr;
   int l_diag = 0;  // 1: aiL divides by the stored diagonal of a lower triangular matrix
   // general ISAI: per row the sz*sz positions of A(J_k, J_t) in the factor
   // pattern (row-major over k, -1 = structural zero), and the position of i in J
@@ -358,7 +358,7 @@ struct bilu_plan {
   int pl_ndep = 0, pl_nlow = 0;
   bool has_isai = false;
   std::vector<int> ail_rp, ail_ci, aiu_rp, aiu_ci;
-  std::vector<int> ail_prog_ptr, ail_prog, aiu_prog_ptr, aiu_prog;  // prog in int units (pairs)
+  std::vector<int> ail_prog_ptr, ail_prog, aiu_prog_ptr, aiu_prog;  // per-row programs, one word per step
   bool general_isai = false;
   std::vector<int> gen_map_ptr, gen_map, gen_pos;
   int* dbuf = nullptr;

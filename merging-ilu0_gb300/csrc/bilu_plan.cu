@@ -303,9 +303,15 @@ bilu_status build_isai_general(bilu_plan& P) {
   return BILU_OK;
 }
 
+// Per-row ISAI programs, one 32-bit word per step: a header t | count << 5
+// (the unknown solved next and how many products it takes), then per product
+// c | pos << 5 (the unknown it reads and the factor entry's position).  Rows
+// have at most 32 entries, so t, count and c take 5 bits; pos needs nnz < 2^26.
 bilu_status build_isai(bilu_plan& P) {
   if (P.general_isai) return build_isai_general(P);
   const int n = P.n;
+  if (P.nnz >= (1 << 26))
+    return set_error(BILU_ERR_CAPACITY, "ISAI: factor patterns of 2^26 or more entries are not supported");
   const int power = std::max(1, P.opts.isai_power);
   pattern_power(n, P.l_rp, P.l_ci, power, P.ail_rp, P.ail_ci);
   pattern_power(n, P.u_rp, P.u_ci, power, P.aiu_rp, P.aiu_ci);
@@ -321,19 +327,17 @@ bilu_status build_isai(bilu_plan& P) {
     for (int t = sz - 2; t >= 0; --t) {
       const size_t hdr = P.ail_prog.size();
       P.ail_prog.push_back(t);
-      P.ail_prog.push_back(0);
       int cnt = 0;
       for (int c = sz - 1; c > t; --c) {
         const int pos = find_pos(P.rp, P.ci, P.ail_ci[beg + c], P.ail_ci[beg + t]);
         if (pos >= 0) {
-          P.ail_prog.push_back(c);
-          P.ail_prog.push_back(pos);
+          P.ail_prog.push_back(c | pos << 5);
           ++cnt;
         }
       }
-      P.ail_prog[hdr + 1] = cnt;
+      P.ail_prog[hdr] = t | cnt << 5;
     }
-    P.ail_prog_ptr[i + 1] = (int)(P.ail_prog.size() / 2);
+    P.ail_prog_ptr[i + 1] = (int)P.ail_prog.size();
   }
   P.aiu_prog_ptr.assign(n + 1, 0);
   P.aiu_prog.clear();
@@ -346,19 +350,17 @@ bilu_status build_isai(bilu_plan& P) {
     for (int t = 1; t < sz; ++t) {
       const size_t hdr = P.aiu_prog.size();
       P.aiu_prog.push_back(t);
-      P.aiu_prog.push_back(0);
       int cnt = 0;
       for (int c = 0; c < t; ++c) {
         const int pos = find_pos(P.rp, P.ci, P.aiu_ci[beg + c], P.aiu_ci[beg + t]);
         if (pos >= 0) {
-          P.aiu_prog.push_back(c);
-          P.aiu_prog.push_back(pos);
+          P.aiu_prog.push_back(c | pos << 5);
           ++cnt;
         }
       }
-      P.aiu_prog[hdr + 1] = cnt;
+      P.aiu_prog[hdr] = t | cnt << 5;
     }
-    P.aiu_prog_ptr[i + 1] = (int)(P.aiu_prog.size() / 2);
+    P.aiu_prog_ptr[i + 1] = (int)P.aiu_prog.size();
   }
   return BILU_OK;
 }
@@ -521,7 +523,7 @@ bilu_status upload(bilu_plan& P) {
     o_aurp = put(P.aiu_rp);
     o_auci = put(P.aiu_ci);
     // device layout of the per-row ISAI programs: rows in blocks of 32 (a warp's rows), word j of
-    // row 32b+l at off[b] + 32j + l (int2 units), so a warp's program loads are contiguous lines
+    // row 32b+l at off[b] + 32j + l, so a warp's program loads are contiguous lines
     auto blocked = [&](const std::vector<int>& ptr, const std::vector<int>& prog, std::vector<int>& off,
                        std::vector<int>& words) {
       const int nb = (P.n + 31) / 32;
@@ -531,13 +533,9 @@ bilu_status upload(bilu_plan& P) {
         for (int i = 32 * bk; i < std::min(P.n, 32 * bk + 32); ++i) len = std::max(len, ptr[i + 1] - ptr[i]);
         off[bk + 1] = off[bk] + 32 * len;
       }
-      words.assign(2 * (size_t)off[nb], 0);
+      words.assign((size_t)off[nb], 0);
       for (int i = 0; i < P.n; ++i)
-        for (int j = 0; j < ptr[i + 1] - ptr[i]; ++j) {
-          const size_t dst = 2 * ((size_t)off[i / 32] + 32 * j + i % 32);
-          words[dst] = prog[2 * (ptr[i] + j)];
-          words[dst + 1] = prog[2 * (ptr[i] + j) + 1];
-        }
+        for (int j = 0; j < ptr[i + 1] - ptr[i]; ++j) words[(size_t)off[i / 32] + 32 * j + i % 32] = prog[ptr[i] + j];
     };
     std::vector<int> off, words;
     blocked(P.ail_prog_ptr, P.ail_prog, off, words);
@@ -627,9 +625,9 @@ bilu_status upload(bilu_plan& P) {
     d.aiu_rp = b + o_aurp;
     d.aiu_ci = b + o_auci;
     d.ail_prog_ptr = b + o_alpp;
-    d.ail_prog = reinterpret_cast<const int2*>(b + o_alp);
+    d.ail_prog = b + o_alp;
     d.aiu_prog_ptr = b + o_aupp;
-    d.aiu_prog = reinterpret_cast<const int2*>(b + o_aup);
+    d.aiu_prog = b + o_aup;
   }
   if (P.general_isai) {
     d.gen_map_ptr = b + o_gmp;

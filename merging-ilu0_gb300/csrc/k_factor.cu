@@ -238,15 +238,16 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
     m[sz - 1] = P.l_diag ? 1.0 / LU[__ldg(P.diag + i)] : 1.0;
     int q = __ldg(P.ail_prog_ptr + (i >> 5)) + (i & 31);
     for (int blk = 0; blk < sz - 1; ++blk) {
-      const int2 h = __ldg(P.ail_prog + q);  // {t, count}; a row's words are 32 apart
+      const int h = __ldg(P.ail_prog + q);  // t | count << 5; a row's words are 32 apart
+      const int ht = h & 31, hc = h >> 5;
       q += 32;
       double acc = 0.0;
-      for (int u = 0; u < h.y; ++u) {
-        const int2 e = __ldg(P.ail_prog + q);  // {c, position in LU}
+      for (int u = 0; u < hc; ++u) {
+        const int e = __ldg(P.ail_prog + q);  // c | position in LU << 5
         q += 32;
-        acc = fma(-m[e.x], LU[e.y], acc);
+        acc = fma(-m[e & 31], LU[e >> 5], acc);
       }
-      m[h.x] = P.l_diag ? acc / LU[__ldg(P.diag + __ldg(P.ail_ci + beg + h.x))] : acc;
+      m[ht] = P.l_diag ? acc / LU[__ldg(P.diag + __ldg(P.ail_ci + beg + ht))] : acc;
     }
   }
   __syncthreads();
@@ -264,16 +265,17 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
     m[0] = FAST ? rinv[i] : 1.0 / LU[__ldg(P.diag + i)];
     int q = __ldg(P.aiu_prog_ptr + (i >> 5)) + (i & 31);
     for (int blk = 1; blk < sz; ++blk) {
-      const int2 h = __ldg(P.aiu_prog + q);  // {t, count}; a row's words are 32 apart
+      const int h = __ldg(P.aiu_prog + q);  // t | count << 5; a row's words are 32 apart
+      const int ht = h & 31, hc = h >> 5;
       q += 32;
       double acc = 0.0;
-      for (int u = 0; u < h.y; ++u) {
-        const int2 e = __ldg(P.aiu_prog + q);  // {c, position in LU}
+      for (int u = 0; u < hc; ++u) {
+        const int e = __ldg(P.aiu_prog + q);  // c | position in LU << 5
         q += 32;
-        acc = fma(-m[e.x], LU[e.y], acc);
+        acc = fma(-m[e & 31], LU[e >> 5], acc);
       }
-      const int jt = __ldg(P.aiu_ci + beg + h.x);
-      m[h.x] = FAST ? acc * rinv[jt] : acc / LU[__ldg(P.diag + jt)];
+      const int jt = __ldg(P.aiu_ci + beg + ht);
+      m[ht] = FAST ? acc * rinv[jt] : acc / LU[__ldg(P.diag + jt)];
     }
   }
   __syncthreads();
@@ -305,15 +307,16 @@ __global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, 
     m[sz - 1] = 1.0f;
     int q = __ldg(P.ail_prog_ptr + (i >> 5)) + (i & 31);
     for (int blk = 0; blk < sz - 1; ++blk) {
-      const int2 h = __ldg(P.ail_prog + q);  // {t, count}; a row's words are 32 apart
+      const int h = __ldg(P.ail_prog + q);  // t | count << 5; a row's words are 32 apart
+      const int ht = h & 31, hc = h >> 5;
       q += 32;
       float acc = 0.0f;
-      for (int u = 0; u < h.y; ++u) {
-        const int2 e = __ldg(P.ail_prog + q);  // {c, position in LU}
+      for (int u = 0; u < hc; ++u) {
+        const int e = __ldg(P.ail_prog + q);  // c | position in LU << 5
         q += 32;
-        acc = fmaf(-m[e.x], LU[e.y], acc);
+        acc = fmaf(-m[e & 31], LU[e >> 5], acc);
       }
-      m[h.x] = acc;
+      m[ht] = acc;
     }
   }
   __syncthreads();
@@ -328,15 +331,16 @@ __global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, 
     m[0] = rinv[i];
     int q = __ldg(P.aiu_prog_ptr + (i >> 5)) + (i & 31);
     for (int blk = 1; blk < sz; ++blk) {
-      const int2 h = __ldg(P.aiu_prog + q);  // {t, count}; a row's words are 32 apart
+      const int h = __ldg(P.aiu_prog + q);  // t | count << 5; a row's words are 32 apart
+      const int ht = h & 31, hc = h >> 5;
       q += 32;
       float acc = 0.0f;
-      for (int u = 0; u < h.y; ++u) {
-        const int2 e = __ldg(P.aiu_prog + q);  // {c, position in LU}
+      for (int u = 0; u < hc; ++u) {
+        const int e = __ldg(P.aiu_prog + q);  // c | position in LU << 5
         q += 32;
-        acc = fmaf(-m[e.x], LU[e.y], acc);
+        acc = fmaf(-m[e & 31], LU[e >> 5], acc);
       }
-      m[h.x] = acc * rinv[__ldg(P.aiu_ci + beg + h.x)];
+      m[ht] = acc * rinv[__ldg(P.aiu_ci + beg + ht)];
     }
   }
   __syncthreads();
