@@ -282,6 +282,29 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
   for (int k = threadIdx.x; k < P.aiu_nnz; k += blockDim.x) aiu[(size_t)sys * P.aiu_nnz + k] = (FT)M[k];
 }
 
+// The products of one block of a row's FP32 ISAI program (fmaf from 0 in
+// program order), advancing q past it.  The entries are loaded four at a time
+// so that their latencies overlap.
+__device__ __forceinline__ float isai_block_f32(const int* __restrict__ prog, int& q, int hc, const float* m,
+                                                const float* LU) {
+  float acc = 0.0f;
+  int u = 0;
+  for (; u + 4 <= hc; u += 4) {
+    int e[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) e[j] = __ldg(prog + q + 32 * j);  // c | position in LU << 5
+    q += 128;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc = fmaf(-m[e[j] & 31], LU[e[j] >> 5], acc);
+  }
+  for (; u < hc; ++u) {
+    const int e = __ldg(prog + q);
+    q += 32;
+    acc = fmaf(-m[e & 31], LU[e >> 5], acc);
+  }
+  return acc;
+}
+
 // FAST ISAI stored in FP32 (BILU_REDUCE_FAST with BILU_FP32), computed in
 // FP32: the factors are rounded to float once into shared memory, every
 // product is an fmaf in the order of k_isai's program, and the aiU entries are
@@ -306,17 +329,13 @@ __global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, 
     float* m = M + beg;
     m[sz - 1] = 1.0f;
     int q = __ldg(P.ail_prog_ptr + (i >> 5)) + (i & 31);
+    // blocks 0 .. sz-2; each block's header (t | count << 5) is loaded while the block before it runs
+    int h = sz > 1 ? __ldg(P.ail_prog + q) : 0;
     for (int blk = 0; blk < sz - 1; ++blk) {
-      const int h = __ldg(P.ail_prog + q);  // t | count << 5; a row's words are 32 apart
       const int ht = h & 31, hc = h >> 5;
       q += 32;
-      float acc = 0.0f;
-      for (int u = 0; u < hc; ++u) {
-        const int e = __ldg(P.ail_prog + q);  // c | position in LU << 5
-        q += 32;
-        acc = fmaf(-m[e & 31], LU[e >> 5], acc);
-      }
-      m[ht] = acc;
+      h = blk + 1 < sz - 1 ? __ldg(P.ail_prog + q + 32 * hc) : 0;
+      m[ht] = isai_block_f32(P.ail_prog, q, hc, m, LU);
     }
   }
   __syncthreads();
@@ -330,16 +349,13 @@ __global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, 
     float* m = M + beg;
     m[0] = rinv[i];
     int q = __ldg(P.aiu_prog_ptr + (i >> 5)) + (i & 31);
+    // blocks 1 .. sz-1, headers loaded one block ahead as for aiL
+    int h = sz > 1 ? __ldg(P.aiu_prog + q) : 0;
     for (int blk = 1; blk < sz; ++blk) {
-      const int h = __ldg(P.aiu_prog + q);  // t | count << 5; a row's words are 32 apart
       const int ht = h & 31, hc = h >> 5;
       q += 32;
-      float acc = 0.0f;
-      for (int u = 0; u < hc; ++u) {
-        const int e = __ldg(P.aiu_prog + q);  // c | position in LU << 5
-        q += 32;
-        acc = fmaf(-m[e & 31], LU[e >> 5], acc);
-      }
+      h = blk + 1 < sz ? __ldg(P.aiu_prog + q + 32 * hc) : 0;
+      const float acc = isai_block_f32(P.aiu_prog, q, hc, m, LU);
       m[ht] = acc * rinv[__ldg(P.aiu_ci + beg + ht)];
     }
   }
