@@ -131,6 +131,13 @@ struct DevPattern {
   // pairs (u = a); warps of one class do the same operations
   const int* pl_ent = nullptr;  // nnz
   int pl_ndep = 0, pl_nlow = 0;
+  // the entries with dependency pairs as a warp-blocked program: slot q
+  // (= pl_ent position q < pl_ndep) holds the words k, j << 1 | (j < i), the
+  // pair count, then x, y per pair (sum order); word w of slot 32b + l at
+  // pl_prog[pl_prog_ptr[b] + 32 w + l], so a warp's loads are contiguous and
+  // none waits on another
+  const int* pl_prog_ptr = nullptr;
+  const int* pl_prog = nullptr;
 };
 
 // Shared-memory carve-up of the solver kernel for one system (byte offsets;
@@ -356,6 +363,7 @@ struct bilu_plan {
   std::vector<int> sa_off, sa_ci, sa_src, su_off, su_ci, su_src;  // SELL-32 layouts (DevPattern::sa_*, su_*)
   std::vector<int> pl_ent;  // ParILU entry classes (see DevPattern::pl_ent)
   int pl_ndep = 0, pl_nlow = 0;
+  std::vector<int> pl_prog_ptr, pl_prog;  // ParILU program (DevPattern::pl_prog)
   bool has_isai = false;
   std::vector<int> ail_rp, ail_ci, aiu_rp, aiu_ci;
   std::vector<int> ail_prog_ptr, ail_prog, aiu_prog_ptr, aiu_prog;  // per-row programs, one word per step

@@ -489,6 +489,7 @@ bilu_status upload(bilu_plan& P) {
   const size_t o_lsrc = put(P.l_src), o_usrc = put(P.u_src);
   const size_t o_rlev = put(P.row_lev), o_tpos = put(P.tpos), o_ment = put(P.mlp_ent);
   const size_t o_plent = put(P.pl_ent);
+  const size_t o_plpp = put(P.pl_prog_ptr), o_plp = put(P.pl_prog);
   const size_t o_tlh = put(P.tp_lo_hdr), o_tl = put(P.tp_lo), o_tuh = put(P.tp_up_hdr), o_tu = put(P.tp_up);
   const size_t o_sao = put(P.sa_off), o_sac = put(P.sa_ci), o_sas = put(P.sa_src);
   const size_t o_ih = put(P.ilu_hdr), o_ip = put(P.ilu_prog);
@@ -582,6 +583,8 @@ bilu_status upload(bilu_plan& P) {
   d.n_mlp = (int)P.mlp_ent.size();
   d.mlp_ent = b + o_ment;
   d.pl_ent = b + o_plent;
+  d.pl_prog_ptr = b + o_plpp;
+  d.pl_prog = b + o_plp;
   if (ci16) {
     d.a_ci16 = reinterpret_cast<const unsigned short*>(b + o_a16);
     if (!P.sa_ci.empty()) d.sa_ci16 = reinterpret_cast<const unsigned short*>(b + o_sa16);
@@ -829,6 +832,29 @@ bilu_status bilu_plan_create(bilu_plan** out, int n, int nnz, const int* h_rp, c
     P->pl_ent = with_deps;
     P->pl_ent.insert(P->pl_ent.end(), lower.begin(), lower.end());
     P->pl_ent.insert(P->pl_ent.end(), upper.begin(), upper.end());
+    // the entries with pairs as a warp-blocked program (DevPattern::pl_prog)
+    const int nb = (P->pl_ndep + 31) / 32;
+    P->pl_prog_ptr.assign(nb + 1, 0);
+    for (int bk = 0; bk < nb; ++bk) {
+      int len = 0;
+      for (int q = 32 * bk; q < std::min(P->pl_ndep, 32 * bk + 32); ++q) {
+        const int k = P->pl_ent[q];
+        len = std::max(len, 3 + 2 * (P->dep_ptr[k + 1] - P->dep_ptr[k]));
+      }
+      P->pl_prog_ptr[bk + 1] = P->pl_prog_ptr[bk] + 32 * len;
+    }
+    P->pl_prog.assign(P->pl_prog_ptr[nb], 0);
+    for (int q = 0; q < P->pl_ndep; ++q) {
+      const int k = P->pl_ent[q], i = P->row_of[k], j = P->ci[k];
+      int* w = P->pl_prog.data() + P->pl_prog_ptr[q / 32] + q % 32;
+      w[0] = k;
+      w[32] = j << 1 | (j < i ? 1 : 0);
+      w[64] = P->dep_ptr[k + 1] - P->dep_ptr[k];
+      for (int u = 0; u < w[64]; ++u) {
+        w[96 + 64 * u] = P->dep[2 * (P->dep_ptr[k] + u)];
+        w[128 + 64 * u] = P->dep[2 * (P->dep_ptr[k] + u) + 1];
+      }
+    }
   }
   P->has_isai = is_isai(P->opts.precond);
   P->general_isai = P->opts.precond == BILU_PRECOND_GENERAL_ISAI;

@@ -143,22 +143,27 @@ __global__ void __launch_bounds__(512) k_parilu0(const DevPattern P, int nsys, c
       for (int r = threadIdx.x; r < P.n; r += blockDim.x) rinv[r] = __drcp_rn(cur[__ldg(P.diag + r)]);
       __syncthreads();
     }
-    // entries with dependency pairs (most pairs first, so a warp's lanes run alike)
+    // entries with dependency pairs (most pairs first, so a warp's lanes run
+    // alike), read from the warp-blocked program: the words of a slot do not
+    // depend on one another, so their loads overlap
     for (int q = threadIdx.x; q < P.pl_ndep; q += blockDim.x) {
-      const int k = __ldg(P.pl_ent + q);
-      const int pb = __ldg(P.dep_ptr + k), pe = __ldg(P.dep_ptr + k + 1);
+      const int* w = P.pl_prog + __ldg(P.pl_prog_ptr + (q >> 5)) + (q & 31);
+      const int k = __ldg(w), jl = __ldg(w + 32), cnt = __ldg(w + 64);
+      w += 96;
       double s = 0.0;
-      for (int q2 = pb; q2 < pe; ++q2) {
-        const int2 d = __ldg(P.dep + q2);
-        s = fma(cur[d.x], cur[d.y], s);
+#pragma unroll 4
+      for (int u = 0; u < cnt; ++u) {
+        s = fma(cur[__ldg(w)], cur[__ldg(w + 32)], s);
+        w += 64;
       }
-      const int i = __ldg(P.row_of + k), j = __ldg(P.ci + k);
+      const int j = jl >> 1;
+      const bool low = (jl & 1) != 0;  // j < i
       const double as = __ldg(Ag + k) - s;
       if (track) {  // (A - LU)_ij = (a - s) - l_ij u_jj below the diagonal, (a - s) - u_ij on or above it
-        const double r = (j < i) ? fma(-cur[k], cur[__ldg(P.diag + j)], as) : as - cur[k];
+        const double r = low ? fma(-cur[k], cur[__ldg(P.diag + j)], as) : as - cur[k];
         r2 = fma(r, r, r2);
       }
-      if (!last) nxt[k] = (j < i) ? (FAST ? as * rinv[j] : as / cur[__ldg(P.diag + j)]) : as;
+      if (!last) nxt[k] = low ? (FAST ? as * rinv[j] : as / cur[__ldg(P.diag + j)]) : as;
     }
     // lower entries without pairs: the sum is 0, so l = a / u_jj (a - 0 == a exactly)
     const int lend = P.pl_ndep + P.pl_nlow;
