@@ -26,17 +26,27 @@ def workload(name, nsys, seed=SEED):
 
 
 def oracle_pipeline(rp, ci, vals, b, precond, approach=1, sweeps=5, fp32=False, tol_mode=0, tol=1e-11,
-                    max_iter=500, isai_power=2, lu_init=None):
-    """The reference's computation for one preconditioner family, restated on the CPU."""
+                    max_iter=500, isai_power=2, lu_init=None, patterns=None):
+    """The reference's computation for one preconditioner family, restated on the CPU.
+
+    patterns: an optional dict that keeps the pattern-only work (diagonal insertion, L/U split and ISAI
+    patterns) of the first call for the later calls on the same pattern, as a plan does; timing runs
+    fill it untimed."""
     out = {}
+    memo = patterns if patterns is not None else {}
+
+    def once(key, f):
+        if key not in memo:
+            memo[key] = f()
+        return memo[key]
     if precond == bilu.PRECOND_NONE:
         r = O.bicgstab(rp, ci, vals, b, prec=O.PREC_NONE, dot=0, tol_mode=tol_mode, tol=tol, max_iter=max_iter)
         r["true_res"] = O.true_residual(rp, ci, vals, b, r["x"])
         return r
-    nrp, nci, src = O.add_missing_diag(rp, ci)
+    nrp, nci, src = once("diag", lambda: O.add_missing_diag(rp, ci))
     fvals = np.where(src[None, :] >= 0, vals[:, np.maximum(src, 0)], 0.0)
     if precond == bilu.PRECOND_GENERAL_ISAI:
-        arp, aci = O.isai_pattern(nrp, nci, isai_power)
+        arp, aci = once("gisai", lambda: O.isai_pattern(nrp, nci, isai_power))
         ai = O.isai_values(nrp, nci, fvals, 2, arp, aci)
         out.update(ai=ai, ai_pattern=(arp, aci))
         if fp32:
@@ -54,10 +64,10 @@ def oracle_pipeline(rp, ci, vals, b, precond, approach=1, sweeps=5, fp32=False, 
         lu = O.parilu0(nrp, nci, fvals, sweeps, init=lu_init)
     out["lu"] = lu
     if precond in (bilu.PRECOND_ILU0_ISAI, bilu.PRECOND_PARILU0_ISAI):
-        lrp, lci, urp, uci = O.split_pattern(nrp, nci)
+        lrp, lci, urp, uci = once("split", lambda: O.split_pattern(nrp, nci))
         L, U = O.split_values(nrp, nci, lu)
-        arp, aci = O.isai_pattern(lrp, lci, isai_power)
-        brp, bci = O.isai_pattern(urp, uci, isai_power)
+        arp, aci = once("isai_l", lambda: O.isai_pattern(lrp, lci, isai_power))
+        brp, bci = once("isai_u", lambda: O.isai_pattern(urp, uci, isai_power))
         ail = O.isai_values(lrp, lci, L, 0, arp, aci)
         aiu = O.isai_values(urp, uci, U, 1, brp, bci)
         out.update(ail=ail, aiu=aiu, ail_pattern=(arp, aci), aiu_pattern=(brp, bci))

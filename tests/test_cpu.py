@@ -188,3 +188,33 @@ def test_oracle_half_step_exit_and_caps(built):
     assert np.all(r["iters"] == 2) and np.all(r["conv"] == -1)
     r = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_ILU0)
     assert np.all(np.mod(r["iters"] * 2, 1) == 0)  # multiples of 0.5
+
+
+def test_bench_reference_arm_json_line(built):
+    """bench.py --impl reference times the CPU restatement on the host cores and prints the same JSON line
+    as the GPU arm, with impl, cpu_baseline and a zero-copy e2e."""
+    import json
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "systems/s" and line["higher_is_better"] is True
+    assert line["value"] > 0 and line["steps"] == 1
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_oracle_pipeline_pattern_cache_keeps_results(built):
+    """The pattern cache that the CPU timing runs use reproduces the uncached pipeline bit for bit."""
+    rp, ci, v, b = H.workload("3d7_5x5x5", 4)
+    kw = dict(sweeps=3, fp32=True, tol_mode=1, tol=1e-10)
+    want = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_PARILU0_ISAI, **kw)
+    cache = {}
+    H.oracle_pipeline(rp, ci, v[:1], b[:1], bilu.PRECOND_PARILU0_ISAI, patterns=cache, **kw)
+    got = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_PARILU0_ISAI, patterns=cache, **kw)
+    assert set(cache) == {"diag", "split", "isai_l", "isai_u"}
+    for k in ("x", "iters", "res", "true_res", "ail", "aiu"):
+        H.assert_bitwise(got[k], want[k], k)
