@@ -229,6 +229,25 @@ def test_rr_operand_layouts_bitwise(cuda, fam, precond, kw, staging, fp32):
     _check(g, o, f"{fam} precond {precond} staging {staging} fp32={fp32}")
 
 
+@pytest.mark.parametrize("precond,kw", [(bilu.PRECOND_NONE, {}), (bilu.PRECOND_GENERAL_ISAI, dict(isai_power=1)),
+                                       (bilu.PRECOND_PARILU0_ISAI, dict(parilu_sweeps=5))],
+                         ids=["none", "general_isai", "parilu_isai"])
+@pytest.mark.parametrize("fp32", [False, True])
+def test_rr_four_ctas_per_sm_bitwise(cuda, precond, kw, fp32):
+    """The 4-CTAs-per-SM kernel variant (staging bit 4; 8 rows per thread at n = 343) for every
+    preconditioner kind it serves gives the oracle's FAST-order bits."""
+    if precond == bilu.PRECOND_NONE and fp32:
+        pytest.skip("no preconditioner values to round")
+    rp, ci, v, b = H.workload("3d7_7x7x7", NSYS)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, reduction=bilu.REDUCE_FAST, smem_staging=16,
+                    factor_precision=bilu.FP32 if fp32 else bilu.FP64, **kw, **TOL)
+    assert g["info"]["operands_in_smem"] & 16, "the 4-CTA variant was not selected"
+    o = _oracle_fast(rp, ci, v, b, precond, g["info"]["threads"], fp32, sweeps=kw.get("parilu_sweeps", 5),
+                     power=kw.get("isai_power", 2), **TOL)
+    _check(g, o, f"4 CTAs per SM, precond {precond} fp32={fp32}")
+    assert np.all(g["conv"] == 1)
+
+
 def _wide_level_pattern(n=1000, seed=5):
     """Rows with a diagonal, upper entries (i, i+1) and (i, i+7), and lower entries only in every 97th row:
     the lower solve (and the ILU(0) schedule) has a first level of ~990 rows, far wider than the CTA, and
