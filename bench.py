@@ -12,8 +12,16 @@ sides and the device->host copy of the solutions and per-system results.
 
 Under torchrun (N > 1) rank r solves systems r*B .. (r+1)*B-1 of one seeded
 global batch on its own GPU (shard.py; weak scaling, no collective on the data
-path); the step time is the maximum over ranks.  --impl reference times the CPU restatement of the reference's
-solver (the reference has no CPU path of its own) on the host cores.
+path); the step time is the maximum over ranks.
+
+--impl reference times the CPU restatement of the reference's solver (the
+reference has no CPU path of its own: ILU_0_Factorization_Cpu is declared at
+ILU_0.h:7 and never defined) on all host cores, on the same headline batch and
+config, 4096 systems per step.  Its line also carries the reference's own GPU
+kernels (compiled from its sources into oracle/_ref) timed on the one workload
+they can run: the merged ILU(0) BiCGSTAB of 16384 2D 5-point 16x16 systems
+(the reference's solvers need n <= 512 and, for ISAI, n <= 54 by their static
+shared memory, so they cannot run the headline's n = 1000).
 """
 import argparse
 import json
@@ -67,6 +75,14 @@ SECONDARY = [
          desc="plain form in the reference's operation order (bit-identical iterates; register-resident one-warp "
               "kernel)",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=0)),
+    dict(name="ref_rule_merged_ilu0_2d5_16x16_ref", kind=1, grid=(16, 16, 1), nsys=16384,
+         desc="the reference merged kernel's workload and stopping rule (absolute 1e-11 on the recursive residual, "
+              "500 iterations): merged FP64 ILU(0) BiCGSTAB of 16384 2D 5-point 16x16 systems in the reference's "
+              "operation order (bit-identical to the reference kernel)",
+         opts=dict(precond=0, tol_mode=0, tol=1e-11, reduction=0)),
+    dict(name="ref_rule_merged_ilu0_2d5_16x16_fast", kind=1, grid=(16, 16, 1), nsys=16384,
+         desc="the same batch and stopping rule in FAST order (register-resident kernel)",
+         opts=dict(precond=0, tol_mode=0, tol=1e-11, reduction=1)),
     dict(name="fp32_isai_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768, autotune=True,
          desc="ILU(0) + ISAI stored and applied in FP32 (FP64 A*x, inner products, recurrences), 32768 "
               "convection-diffusion systems 24x24",
@@ -85,6 +101,14 @@ SECONDARY = [
 # through L1: smem_staging 16): ncu dram__bytes_read.sum + dram__bytes_write.sum of a 3072-system
 # launch (430.4 + 38.0 MB) / 3072; the traffic grows in proportion to the systems of a launch.
 RR_TRAFFIC_BYTES_PER_SYSTEM = 152_460
+# the same capture's FP64-pipe figure, sm__pipe_fp64_cycles_active (percent of peak sustained elapsed)
+RR_NCU = {"kernel": "k_bicgstab_rr_occ4<1, float>", "sm__pipe_fp64_cycles_active_pct": 53.8,
+          "dram_bytes_per_system": RR_TRAFFIC_BYTES_PER_SYSTEM,
+          "source": "profiles/k_bicgstab_rr_occ4_parilu5_isai_fp32_3d7_10x10x10.md (3072 systems)"}
+
+# systems of the headline workload that both CPU timings run (the GPU line's cpu_baseline and every step of
+# --impl reference): the whole 4096-system batch, so that the two samples are the same work
+CPU_SAMPLE = 4096
 
 
 def bytes_per_system(n, nnz):
@@ -117,6 +141,49 @@ def load_peaks():
         d = json.load(open(p))
         return d.get("hbm_gbs", 6800.0), "measured"
     return 6800.0, "fallback"
+
+
+def cpu_info():
+    """Host cores and CPU model name of the machine the CPU timings run on."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            for ln in open("/proc/cpuinfo"):
+                if ln.lower().startswith("model name"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    import platform
+    return {"nproc": os.cpu_count(), "model": model or platform.processor() or platform.machine(),
+            "arch": platform.machine()}
+
+
+def headline_config(world=1):
+    """The `config` of both arms' JSON lines (the same workload, so the same dict)."""
+    import bilu
+    kind, (gx, gy, gz) = HEADLINE["kind"], HEADLINE["grid"]
+    rp, ci, _, _ = bilu.gen_stencil(kind, gx, gy, gz, 0, SEED)
+    n, nnz, nsys = len(rp) - 1, len(ci), HEADLINE["nsys"]
+    fp32 = HEADLINE["opts"].get("factor_precision", 0) == 1
+    return {"workload": HEADLINE["desc"], "nsys": nsys, "n": n, "nnz": nnz,
+            "reduction": "fast" if HEADLINE["opts"].get("reduction", 0) == 1 else "reference",
+            "factor_precision": "fp32 ISAI (FP64 A*x, inner products, recurrences, ParILU)" if fp32 else "fp64",
+            "l2": "inputs larger than L2: A values %.0f MB per step" % (nsys * nnz * 8 / 1e6),
+            "parallelism": f"weak: {world} slab(s) of {nsys} systems of one seeded batch, one per GPU, "
+                           f"no collective on the data path"}
+
+
+def headline_dtype():
+    return "f64 (ISAI FP32)" if HEADLINE["opts"].get("factor_precision", 0) == 1 else "f64"
 
 
 class ClockSampler:
@@ -182,31 +249,95 @@ def cpu_port_rate(wl, sample, threads=None):
     return sample / dt, dt, O.num_threads(), float(r["iters"].mean())
 
 
+def reference_gpu_kernels(steps, warmup):
+    """The reference's own merged ILU(0) BiCGSTAB kernel (PrecondBiCGSTAB_exact_ilu0_app1_merged_gpu.cu:249-538,
+    compiled from its sources into oracle/_ref, launched as its helper does at :568-577) on 16384 2D 5-point 16x16
+    systems with the reference's stopping rule (absolute 1e-11 on the recursive residual, 500 iterations), timed
+    with CUDA events.  Its busy-wait triangular solves need n <= 512 and converging systems, so it runs only
+    after the oracle's reference-order solve of the same batch has converged everywhere with finite values."""
+    try:
+        import torch
+        import ref as R
+    except ImportError as ex:
+        return {"unavailable": f"import failed: {ex}"}
+    if not torch.cuda.is_available():
+        return {"unavailable": "no CUDA device"}
+    if not R.available():
+        return {"unavailable": "reference kernels not built (oracle/_ref; oracle/build_ref.py builds them where the "
+                               "reference sources are present)"}
+    import bilu
+    import helpers as H
+    import oracle as O
+    nsys = 16384
+    rp, ci, v, b = bilu.gen_stencil(1, 16, 16, 1, nsys, SEED)
+    n, nnz = len(rp) - 1, len(ci)
+    gate = H.oracle_pipeline(rp, ci, v, b, bilu.PRECOND_ILU0, tol_mode=0, tol=1e-11, max_iter=500)
+    if not (np.all(gate["conv"] == 1) and np.all(np.isfinite(gate["x"]))):
+        return {"unavailable": "the oracle's reference-order solve did not converge everywhere: the reference's "
+                               "busy-wait triangular solves are not run on this batch"}
+    dev = torch.device("cuda", 0)
+    T = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    RP, CI, D = T(rp, torch.int32), T(ci, torch.int32), T(O.find_diag(rp, ci), torch.int32)
+    V, B = T(v, torch.float64), T(b, torch.float64)
+    X = torch.zeros_like(B)
+    F = torch.empty_like(V)
+    it = torch.zeros(nsys, dtype=torch.float32, device=dev)
+    cv = torch.zeros(nsys, dtype=torch.int32, device=dev)
+    rs = torch.zeros(nsys, dtype=torch.float64, device=dev)
+    L = R.lib()
+    args = (L.ref_merged, n, nnz, nsys, RP, CI, V, B, X, F, D, it, cv, rs)
+    for _ in range(max(warmup, 1)):
+        R._call(*args)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        R._call(*args)  # the reference's kernel on the legacy default stream (torch's current stream here)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    iters = it.cpu().numpy()
+    same = bool(np.array_equal(iters, gate["iters"]) and np.array_equal(X.cpu().numpy(), gate["x"]))
+    return {"workload": "merged ILU(0) BiCGSTAB (the reference's namesake kernel), 16384 FP64 systems, 2D 5-point "
+                        "16x16 (n=256, nnz=1216), absolute tol 1e-11 on the recursive residual, max 500 iterations",
+            "kernel": "KernelBatchedPreconditionedBiCGSTAB_ILU (PrecondBiCGSTAB_exact_ilu0_app1_merged_gpu.cu), "
+                      "built for sm_103a from the reference sources, 16384 CTAs of 512 threads",
+            "systems_per_s": nsys / (ms / 1e3), "ms_per_step": ms, "steps": steps, "mean_iters": float(iters.mean()),
+            "converged": int((cv == 1).sum().item()), "bit_identical_to_oracle_reference_order": same,
+            "compare_with": "the GPU arm's secondary lines ref_rule_merged_ilu0_2d5_16x16_ref and _fast: the library "
+                            "on the same batch and stopping rule"}
+
+
 def run_reference_arm(args):
-    """--impl reference: the CPU restatement of the reference's solver on the host cores."""
+    """--impl reference: the CPU restatement of the reference's solver on all host cores, on the headline
+    batch (CPU_SAMPLE systems per step); the reference's own GPU kernels on the one workload they can run."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     import oracle as O
     wl = HEADLINE
-    sample = 512
     for _ in range(args.warmup):
-        cpu_port_rate(wl, 8)
+        cpu_port_rate(wl, 64)
     rates, secs = [], []
     for _ in range(args.steps):
-        rate, dt, cores, _ = cpu_port_rate(wl, sample)
+        rate, dt, cores, _ = cpu_port_rate(wl, CPU_SAMPLE)
         rates.append(rate)
         secs.append(dt)
     value = statistics.median(rates)
+    host = cpu_info()
     line = {"metric": METRIC, "value": value, "unit": "systems/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * statistics.median(secs),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": wl["desc"], "nsys_per_step": sample},
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": headline_dtype(),
+            "data": "synthetic", "config": headline_config(int(os.environ.get("WORLD_SIZE", "1"))),
             "cpu_baseline": {"value": value, "unit": "systems/s", "cores": O.num_threads(), "kind": "port",
-                             "sample": f"{sample} systems of the headline workload per step, full pipeline "
-                                       f"(ParILU sweeps, ISAI, BiCGSTAB) in the reference's operation order; the "
-                                       f"pattern work runs once, untimed, as in the GPU arm's plan"},
-            "e2e": {"value": value, "unit": "systems/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "host": host,
+                             "sample": f"the headline batch ({CPU_SAMPLE} systems) per step, full pipeline (ParILU "
+                                       f"sweeps, ISAI, BiCGSTAB) in the reference's operation order, OpenMP over "
+                                       f"systems on {O.num_threads()} threads of {host['nproc']} host cores "
+                                       f"({host['model']}); the pattern work runs once per step, untimed, as in "
+                                       f"the GPU arm's plan; value = median over the steps"},
+            "e2e": {"value": value, "unit": "systems/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_gpu_kernels": reference_gpu_kernels(args.steps, args.warmup)}
     print(json.dumps(line))
 
 
@@ -330,13 +461,14 @@ def measure(wl, steps, warmup, dev, stream, sampler=None, e2e=False, timed_hook=
     return out
 
 
-def measure_uneven(dev, stream, nsys=8192, steps=3, warmup=2):
+def measure_uneven(dev, stream, nsys=8192, steps=3, warmup=2, fp32=False):
     """Uneven batch: 8192 systems, n log-uniform in [64, 1024], own random pattern each (5-12 off-diagonals
-    per row), merged ILU(0), FAST order, rel. tol 1e-10; autotuned buckets, one CUDA-graph launch per step."""
+    per row), merged ILU(0) with FP64 (plain) or FP32-stored factors, FAST order, rel. tol 1e-10; autotuned
+    buckets, one CUDA-graph launch per step."""
     import torch
     import bilu
     sn, sz, rp, ci, v, b = bilu.gen_uneven(nsys, SEED, 64, 1024, 5, 12)
-    plan = bilu.UnevenPlan(sn, sz, rp, ci, tol_mode=1, tol=1e-10, reduction=1)
+    plan = bilu.UnevenPlan(sn, sz, rp, ci, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1 if fp32 else 0)
     V = torch.from_numpy(v).to(dev)
     B = torch.from_numpy(b).to(dev)
     X = torch.empty_like(B)
@@ -360,15 +492,16 @@ def measure_uneven(dev, stream, nsys=8192, steps=3, warmup=2):
     info = plan.info()
     plan.close()
     bpsys = (12 * sz + 20 * sn + 4 + 28).astype(np.float64)  # values+cols, b/x/row ptrs, results
-    return {"name": "uneven_ilu0_n64_1024", "nsys": nsys, "systems_per_s": nsys * steps / (ms / 1e3),
+    return {"name": "uneven_ilu0_n64_1024" + ("_fp32" if fp32 else ""), "nsys": nsys, "steps": steps,
+            "systems_per_s": nsys * steps / (ms / 1e3),
             "ms_per_step": ms / steps, "mean_iters": float(it.mean().item()), "converged": int((cv == 1).sum().item()),
             "mean_n": float(sn.mean()), "total_nnz": int(sz.sum()), "bytes_per_step": float(bpsys.sum()),
             "buckets": [{k: i[k] for k in ("n_hi", "systems", "threads", "grid", "smem_bytes", "tuned_ms")}
                         for i in info if i["systems"]],
             "workload": "uneven batch: 8192 FP64 systems, n log-uniform in [64,1024], 5-12 random off-diagonals per "
-                        "row, diag 1.2x abs row sum with random sign, merged ILU(0), FAST order (register-resident "
-                        "solver, one CTA per system), rel 1e-10, autotuned threads per system per size bucket, one "
-                        "CUDA-graph launch per step"}
+                        "row, diag 1.2x abs row sum with random sign, merged ILU(0) with %s factors, FAST order "
+                        "(register-resident solver, one CTA per system), rel 1e-10, autotuned threads per system per "
+                        "size bucket, one CUDA-graph launch per step" % ("FP32-stored" if fp32 else "FP64")}
 
 
 def measure_learned(dev, stream, ntrain=65536, neval=16384, train_steps=1500, batch=65536, steps=3):
@@ -533,23 +666,26 @@ def main():
     if rank == 0 and not args.quick:
         for wl in SECONDARY:
             try:
-                r = measure(wl, 2, 1, dev, stream)
-                secondary.append({k: r[k] for k in ("name", "nsys", "systems_per_s", "setup_ms", "solve_ms",
+                r = measure(wl, args.steps, max(args.warmup, 1), dev, stream)
+                secondary.append({k: r[k] for k in ("name", "nsys", "steps", "systems_per_s", "setup_ms", "solve_ms",
                                                     "mean_iters", "converged", "max_rel_true_res",
                                                     "forward_error")} |
                                  {"workload": wl["desc"]})
             except Exception as ex:  # a secondary workload never hides the headline
                 secondary.append({"name": wl["name"], "error": str(ex)})
+        for f32 in (False, True):
+            try:
+                secondary.append(measure_uneven(dev, stream, steps=args.steps, warmup=max(args.warmup, 1), fp32=f32))
+            except Exception as ex:
+                secondary.append({"name": "uneven_ilu0_n64_1024" + ("_fp32" if f32 else ""), "error": str(ex)})
         try:
-            secondary.append(measure_uneven(dev, stream))
-        except Exception as ex:
-            secondary.append({"name": "uneven_ilu0_n64_1024", "error": str(ex)})
-        try:
-            secondary.append(measure_learned(dev, stream))
+            secondary.append(measure_learned(dev, stream, steps=args.steps))
         except Exception as ex:
             secondary.append({"name": "learned_warm_start_3d7_7x7x7", "error": str(ex)})
     if rank != 0:
         return
+    # FP64 FMA issue rate of this GPU, measured now (bilu_probe_fp64_rate): the FP64 roofline's peak
+    fp64_peak = bilu.probe_fp64_rate()
     chosen = {}
     by_name = {sc.get("name"): sc for sc in secondary if "systems_per_s" in sc}
     plain = by_name.get("plain_ilu0_3d7_10x10x10")
@@ -560,7 +696,7 @@ def main():
         chosen["headline_3d7_10x10x10"] = {
             "workload": HEADLINE["desc"], "plain_form": "merged FP64 ILU(0) + BiCGSTAB on the same systems",
             "plain_systems_per_s": plain["systems_per_s"],
-            "plain_roofline_fp64_frac": pfl / (plain["solve_ms"] / 1e3) / 1e9 / 1205.0,
+            "plain_roofline_fp64_frac": pfl / (plain["solve_ms"] / 1e3) / 1e9 / fp64_peak,
             "chosen_form": "ParILU(5) + ISAI stored and applied in FP32, register-resident solver",
             "chosen_systems_per_s": res["systems_per_s"], "ratio": res["systems_per_s"] / plain["systems_per_s"]}
         f32 = by_name.get("fp32_ilu0_3d7_10x10x10")
@@ -588,6 +724,13 @@ def main():
             "workload": "32768 convection-diffusion systems 24x24", "plain_form": "merged FP64 ILU(0) + BiCGSTAB",
             "plain_systems_per_s": p24["systems_per_s"], "chosen_form": "ILU(0) + ISAI stored and applied in FP32",
             "chosen_systems_per_s": i24["systems_per_s"], "ratio": i24["systems_per_s"] / p24["systems_per_s"]}
+    pu, fu = by_name.get("uneven_ilu0_n64_1024"), by_name.get("uneven_ilu0_n64_1024_fp32")
+    if pu and fu:
+        chosen["uneven_n64_1024"] = {
+            "workload": "8192 uneven systems (n log-uniform in [64,1024], own random pattern each), one CUDA-graph "
+                        "launch per step", "plain_form": "merged FP64 ILU(0) + BiCGSTAB",
+            "plain_systems_per_s": pu["systems_per_s"], "chosen_form": "merged ILU(0), FP32-stored factors",
+            "chosen_systems_per_s": fu["systems_per_s"], "ratio": fu["systems_per_s"] / pu["systems_per_s"]}
     for sc in secondary:
         if sc.get("name") == "learned_warm_start_3d7_7x7x7" and "learned" in sc:
             chosen["learned_3d7_7x7x7"] = {
@@ -606,41 +749,44 @@ def main():
     fp32_prec = HEADLINE["opts"].get("factor_precision", 0) == 1
     prec_nnz = 0 if fp32_prec else info["nnz_isai_L"] + info["nnz_isai_U"]  # FP32 ISAI work is not FP64
     flops = fp64_flops_per_iter(n, nnz, prec_nnz, HEADLINE["opts"]["precond"]) * res["mean_iters"] * nsys
-    fp64_peak = 1205.0  # GFLOP/s: 602.5 G DFMA/s measured on this machine's GB300 (full-warp DFMA stream)
-    cores = os.cpu_count()
-    cpu_sample = 4096  # the headline batch: about 10-15 s of CPU work on 16 cores
-    rate, dt, used, _ = cpu_port_rate(HEADLINE, cpu_sample)
+    host = cpu_info()
+    rate, dt, used, _ = cpu_port_rate(HEADLINE, CPU_SAMPLE)
+    kernel = (("k_bicgstab_rr_occ4 (register-resident solver, 4 CTAs per SM)" if info["operands_in_smem"] & 16
+               else "k_bicgstab_rr (register-resident solver)") if info["solver_kernel"] == 1 else "k_bicgstab (solver)")
+    autotuned_occ4 = info["solver_kernel"] == 1 and fp32_prec and bool(info["operands_in_smem"] & 16)
     line = {
         "metric": METRIC, "value": value, "unit": "systems/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": HEADLINE["desc"], "nsys": nsys, "n": n, "nnz": nnz, "reduction": "fast",
-                   "factor_precision": "fp32 ISAI (FP64 A*x, inner products, recurrences, ParILU)" if fp32_prec
-                   else "fp64", "threads_per_system": info["threads"], "solver_kernel": info["solver_kernel"],
-                   "smem_bytes_per_system": info["smem_bytes"],
-                   "l2": "inputs larger than L2: A values %.0f MB per step" % (nsys * nnz * 8 / 1e6),
-                   "parallelism": f"weak: {world} slab(s) of {nsys} systems of one seeded batch, one per GPU, "
-                                  f"no collective on the data path"},
+        "vs_baseline": None, "dtype": headline_dtype(), "data": "synthetic",
+        "config": headline_config(world),
+        "kernel_config": {"solver_kernel": kernel, "threads_per_system": info["threads"],
+                          "smem_bytes_per_system": info["smem_bytes"], "smem_staging": info["operands_in_smem"],
+                          "chosen_by": "bilu_plan_autotune on the batch, before the timed region"},
         "clocks": res["clocks"],
         "e2e": res["e2e"],
         "gpu_launches": launches_per_step(info) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": RR_TRAFFIC_BYTES_PER_SYSTEM * nsys if info["solver_kernel"] == 1 and fp32_prec
-                     else None, "traffic_source": "ncu capture of 3072 systems, scaled per system", "peak_kind": peak_kind, "kernel": ("k_bicgstab_rr_occ4 (register-resident solver, 4 CTAs per SM)" if info["operands_in_smem"] & 16
-                                else "k_bicgstab_rr (register-resident solver)") if info["solver_kernel"] == 1
-                     else "k_bicgstab (solver)",
-                     "bytes_per_system": bps},
+                     "traffic": RR_TRAFFIC_BYTES_PER_SYSTEM * nsys if autotuned_occ4 else None,
+                     "traffic_source": RR_NCU["source"] + ", scaled per system", "peak_kind": peak_kind,
+                     "kernel": kernel, "bytes_per_system": bps,
+                     "achieved_from": "bytes_per_system x nsys / the solver launch's CUDA-event time (stages_ms.solve)"},
         "roofline_fp64": {"achieved": flops / solve_s / 1e9, "peak": fp64_peak, "unit": "GFLOP/s",
                           "frac": flops / solve_s / 1e9 / fp64_peak,
+                          "peak_kind": "measured in this run: bilu_probe_fp64_rate (independent DFMA chains on every "
+                                       "SM, CUDA events, best of 5 launches)",
+                          "counted": "FP64 operations of the BiCGSTAB iterations (bench.fp64_flops_per_iter x mean "
+                                     "iterations x systems); FP32 ISAI work not counted",
+                          "ncu": RR_NCU if autotuned_occ4 else None,
                           "note": "FP64 issue, not HBM, bounds this kernel on GB300"},
         "stages_ms": {"setup": res["setup_ms"], "solve": res["solve_ms"]},
         "solve_quality": {"mean_iters": res["mean_iters"], "max_iters": res["max_iters"],
                           "converged": res["converged"], "max_rel_true_residual": res["max_rel_true_res"],
                           "forward_error": res["forward_error"]},
-        "cpu_baseline": {"value": rate, "unit": "systems/s", "cores": used, "kind": "port",
-                         "sample": f"{cpu_sample} systems of the headline workload through the CPU restatement "
-                                   f"({dt:.2f} s, {used} OpenMP threads of {cores} host cores; the pattern work "
-                                   f"runs once, untimed, as in the GPU arm's plan)"},
+        "cpu_baseline": {"value": rate, "unit": "systems/s", "cores": used, "kind": "port", "host": host,
+                         "sample": f"the headline batch ({CPU_SAMPLE} systems) through the CPU restatement, the same "
+                                   f"sample as each step of --impl reference ({dt:.2f} s, {used} OpenMP threads of "
+                                   f"{host['nproc']} host cores, {host['model']}; the pattern work runs once, "
+                                   f"untimed, as in the GPU arm's plan)"},
         "chosen_vs_plain": chosen or None,
         "secondary": secondary,
     }

@@ -230,14 +230,17 @@ bilu_status bilu_plan_autotune(bilu_plan* plan, int nsys, const double* d_values
  * For callers that cannot let a solve allocate: a simulation calling the
  * batched solver inside its time-step loop keeps a fixed device-memory
  * footprint set at start-up, and cudaMalloc / cudaFree would also
- * synchronise the device mid-step.  Same kernels and bit-identical results as
- * bilu_solve; the intermediate factors live in one fixed 32 MiB device array
- * per GPU, reserved when the library is loaded and held until exit.  Calls
- * needing more scratch than that are rejected with BILU_ERR_CAPACITY (split
- * the batch).  All calls on a device share the array: calls whose kernels
- * overlap on the GPU race.  The first call on a device looks up the array's
- * device address; make it before any stream capture.  The plan must exist
- * already (bilu_plan_create allocates once). */
+ * synchronise the device mid-step.  Same scratch layout, kernels and
+ * bit-identical results as bilu_solve (the SELL-32 operand copies of the
+ * plan's configuration included); the intermediates (factors, ISAI values,
+ * operand copies) live in one fixed 32 MiB device array per GPU, reserved when
+ * the library is loaded and held until exit.  Calls needing more scratch than
+ * that are rejected with BILU_ERR_CAPACITY (split the batch).  All calls on a
+ * device share the array: calls whose kernels overlap on the GPU race.  The
+ * first call on a device does the set-up (looks up the array's device address,
+ * loading the library's device module there if needed); make it before any
+ * stream capture.  The plan must exist already (bilu_plan_create allocates
+ * once). */
 bilu_status bilu_solve_noalloc(bilu_plan* plan, int nsys, const double* d_values, const double* d_b,
                                double* d_x, const bilu_results* results, void* stream);
 
@@ -378,6 +381,11 @@ const char* bilu_last_error(void);
 const char* bilu_version(void);
 /* Number of CUDA devices visible (0 when none; never fails). */
 int bilu_device_count(void);
+/* FP64 FMA throughput of the current device in GFLOP/s (two FLOPs per FMA),
+ * measured with CUDA events on independent DFMA chains that fill every SM:
+ * the peak against which the FP64 roofline of the solver kernels is quoted.
+ * Synchronises the stream.  No reference counterpart. */
+bilu_status bilu_probe_fp64_rate(double* h_gflops, void* stream);
 
 /* ---------------------------------------------------------------- synthetic inputs */
 /* Seeded generators of the benchmark workloads (host memory; no GPU needed).

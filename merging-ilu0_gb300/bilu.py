@@ -36,6 +36,7 @@ EXPORTED = [
     "bilu_uneven_autotune", "bilu_uneven_solve", "bilu_uneven_get_info", "bilu_forward_error",
     "bilu_mlp_create", "bilu_mlp_destroy", "bilu_mlp_param_count", "bilu_mlp_get_params", "bilu_mlp_set_params",
     "bilu_mlp_train", "bilu_mlp_loss_grad", "bilu_mlp_eval", "bilu_mlp_warm_start", "bilu_mlp_save", "bilu_mlp_load",
+    "bilu_probe_fp64_rate",
 ]
 
 
@@ -118,6 +119,7 @@ def lib():
         L.bilu_mlp_warm_start.argtypes = [vp, vp, i, vp, vp, d, vp, vp, vp]
         L.bilu_mlp_save.argtypes = [vp, C.c_char_p]
         L.bilu_mlp_load.argtypes = [vp, C.c_char_p]
+        L.bilu_probe_fp64_rate.argtypes = [C.POINTER(d), vp]
         L.bilu_plan_enable_timing.argtypes = [vp, i]
         L.bilu_plan_last_timing.argtypes = [vp, C.POINTER(Timing)]
         L.bilu_gen_uneven.argtypes = [i, C.c_uint64, i, i, i, i, ip, ip, ip, ip, C.POINTER(d), C.POINTER(d)]
@@ -167,6 +169,13 @@ def device_count():
 
 def version():
     return lib().bilu_version().decode()
+
+
+def probe_fp64_rate(stream=None):
+    """FP64 FMA throughput of the current device, GFLOP/s (bilu_probe_fp64_rate)."""
+    g = C.c_double()
+    _check(lib().bilu_probe_fp64_rate(C.byref(g), _stream(stream)))
+    return g.value
 
 
 # ---------------------------------------------------------------- generators

@@ -343,6 +343,21 @@ cudaError_t launch_split(const DevPattern& p, int nsys, const double* lu, double
 cudaError_t launch_true_residual(const DevPattern& p, int nsys, const double* A, const double* b, const double* x,
                                  double* out, int threads, cudaStream_t st);
 
+// Scratch of one solve (intermediate factors, ISAI values, SELL-32 copies of
+// the solver's operands): 256-byte aligned byte offsets into one workspace,
+// the plan's own (bilu_solve) or the library's fixed array (bilu_solve_noalloc).
+struct SolveScratch {
+  size_t exp = 0, lu = 0, f = 0, ail = 0, aiu = 0, asell = 0, usell = 0, total = 0;
+  bool sell_a = false, sell_u = false;  // the solver reads SELL-32 copies of A / aiU made before its launch
+};
+SolveScratch solve_scratch_layout(const bilu_plan* P, int nsys);
+// The launches of one solve (factorisation, ISAI, SELL-32 copies, solver) with
+// the scratch at ws (solve_scratch_layout(P, nsys).total bytes); allocates nothing.
+bilu_status solve_launch(bilu_plan* P, int nsys, const double* vals, const double* lu_init, const double* b,
+                         double* x, const bilu_results* R, char* ws, const SolveScratch& sc, cudaStream_t st);
+// CTA size of the factorisation and ISAI kernels for a plan
+int fact_threads(const bilu_plan* P);
+
 }  // namespace bilu
 
 // Plan object behind the opaque bilu_plan handle of the C ABI.

@@ -1023,55 +1023,55 @@ bilu_status bilu_expand_values(const bilu_plan* P, int nsys, const double* vin, 
 }  // extern "C"
 
 namespace plan_detail {
-
-// factor-pattern values for the factorisation kernels: the caller's array
-// when no diagonal was inserted, else an expanded copy in `scratch`
 const double* factor_values(bilu_plan* P, int nsys, const double* vin, double* scratch, cudaStream_t st,
-                            cudaError_t* err) {
-  *err = cudaSuccess;
-  if (P->missing == 0) return vin;
-  *err = launch_expand(P->dp, nsys, vin, scratch, st);
-  return scratch;
-}
+                            cudaError_t* err);
+}  // namespace plan_detail
+
+namespace bilu {
 
 int fact_threads(const bilu_plan* P) { return std::min(512, round_up(std::max(P->n, 64), 32)); }
 
-bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double* lu_init, const double* b, double* x,
-                       const bilu_results* R, cudaStream_t st) {
-  if (nsys < 0 || (nsys > 0 && (!vals || !b || !x))) return set_error(BILU_ERR_INVALID, "bilu_solve: bad arguments");
-  if (P->opts.isai_lower_diag)
-    return set_error(BILU_ERR_INVALID, "bilu_solve: plans with isai_lower_diag = 1 only serve bilu_isai");
-  if (nsys == 0) return BILU_OK;
+// Tight scratch of one solve, every region 256-byte aligned: the expanded
+// values (inserted diagonals only), the FP64 factors (ILU / ParILU
+// preconditioners), their FP32 copy (triangular-solve preconditioners with
+// FP32 factors), the ISAI values in the preconditioner's type, and the
+// SELL-32 copies of A and aiU that the register-resident solver reads when its
+// configuration asks for them.
+SolveScratch solve_scratch_layout(const bilu_plan* P, int nsys) {
+  SolveScratch s;
+  const bilu_options& o = P->opts;
+  const int prec = o.precond;
+  const bool fp32 = is_fp32(o);
+  const size_t nz = (size_t)P->nnz * nsys;
+  const bool factors = prec == BILU_PRECOND_ILU0_SPLIT || prec == BILU_PRECOND_PARILU0 ||
+                       prec == BILU_PRECOND_ILU0_ISAI || prec == BILU_PRECOND_PARILU0_ISAI;
+  const bool pre = factors || prec == BILU_PRECOND_GENERAL_ISAI;  // preconditioner generated before the solve
+  const size_t fts = fp32 ? 4 : 8;
+  size_t need = 0;
+  auto take = [&](size_t& off, size_t bytes) {
+    off = need;
+    need += align_up(bytes);
+  };
+  if (pre && P->missing) take(s.exp, nz * 8);
+  if (factors) take(s.lu, nz * 8);
+  if (fp32 && (prec == BILU_PRECOND_ILU0_SPLIT || prec == BILU_PRECOND_PARILU0)) take(s.f, nz * 4);
+  if (P->has_isai) take(s.ail, (size_t)P->dp.ail_nnz * nsys * fts);
+  if (P->has_isai && !P->general_isai) take(s.aiu, (size_t)P->dp.aiu_nnz * nsys * fts);
+  s.sell_a = P->rr && P->rr_sell && P->rr_lay.A < 0 && P->dp.sa_nnz > 0;
+  s.sell_u = P->rr && P->rr_sell && P->rr_pv == 1 && P->rr_lay.aiu < 0 && P->dp.su_nnz > 0;
+  if (s.sell_a) take(s.asell, (size_t)P->dp.sa_nnz * nsys * 8);
+  if (s.sell_u) take(s.usell, (size_t)P->dp.su_nnz * nsys * fts);
+  s.total = need;
+  return s;
+}
+
+bilu_status solve_launch(bilu_plan* P, int nsys, const double* vals, const double* lu_init, const double* b,
+                         double* x, const bilu_results* R, char* ws, const SolveScratch& sc, cudaStream_t st) {
   const bilu_options& o = P->opts;
   const bool fp32 = is_fp32(o);
   const size_t nz = (size_t)P->nnz * nsys;
-  // workspace: [expanded values][LU][LU float | aiL][aiU]
-  size_t need = 0;
-  const size_t off_exp = need;
-  if (P->missing) need += align_up(nz * 8);
-  const size_t off_lu = need;
-  need += align_up(nz * 8);
-  const size_t off_f = need;
-  if (fp32) need += align_up(nz * 4);
-  const size_t off_ail = need;
-  if (P->has_isai) need += align_up((size_t)P->dp.ail_nnz * nsys * 8);
-  const size_t off_aiu = need;
-  if (P->has_isai) need += align_up((size_t)P->dp.aiu_nnz * nsys * 8);
-  // SELL-32 copies read by the register-resident solver: A unless it is staged in shared memory,
-  // aiU of the two-triangle ISAI unless staged
-  const bool sell_a = P->rr && P->rr_sell && P->rr_lay.A < 0 && P->dp.sa_nnz > 0;
-  const bool sell_u = P->rr && P->rr_sell && P->rr_pv == 1 && P->rr_lay.aiu < 0 && P->dp.su_nnz > 0;
-  const size_t off_asell = need;
-  if (sell_a) need += align_up((size_t)P->dp.sa_nnz * nsys * 8);
-  const size_t off_usell = need;
-  if (sell_u) need += align_up((size_t)P->dp.su_nnz * nsys * (fp32 ? 4 : 8));
   const int prec = o.precond;
   if (P->timing) cudaEventRecord(P->ev[0], st);
-  if ((prec != BILU_PRECOND_ILU0 && prec != BILU_PRECOND_NONE) || sell_a) {
-    bilu_status s = ensure_ws(P, need);
-    if (s) return s;
-  }
-  char* ws = (char*)P->ws;
   SolveArgs a;
   a.pat = P->dp;
   a.lay = P->lay;
@@ -1098,42 +1098,42 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
   } else if (prec == BILU_PRECOND_NONE) {
     a.prec = PK_NONE;
   } else {
-    const double* fv = factor_values(P, nsys, vals, (double*)(ws + off_exp), st, &e);
+    const double* fv = factor_values(P, nsys, vals, (double*)(ws + sc.exp), st, &e);
     if (e != cudaSuccess) return cuda_err(e, "expand");
-    double* lu = (double*)(ws + off_lu);
     if (prec == BILU_PRECOND_GENERAL_ISAI) {
-      e = launch_isai_general(P->dp, nsys, fv, ws + off_ail, fp32 ? 1 : 0, ft, st);
+      e = launch_isai_general(P->dp, nsys, fv, ws + sc.ail, fp32 ? 1 : 0, ft, st);
       if (e != cudaSuccess) return cuda_err(e, "general isai");
       a.prec = PK_ISAI;
-      a.ail = ws + off_ail;
+      a.ail = ws + sc.ail;
       a.aiu = nullptr;
     } else {
-    if (prec == BILU_PRECOND_ILU0_SPLIT || prec == BILU_PRECOND_ILU0_ISAI)
-      e = launch_ilu0(P->dp, nsys, fv, lu, o.ilu_approach, ft, st);
-    else
-      e = launch_parilu0(P->dp, nsys, fv, lu_init, lu, o.parilu_sweeps, ft, st, o.parilu_res_tol,
-                         R ? R->parilu_sweeps : nullptr, R ? R->ilu_residual : nullptr,
-                         o.reduction == BILU_REDUCE_FAST ? 1 : 0);
-    if (e != cudaSuccess) return cuda_err(e, "factorisation");
-    if (is_isai(prec)) {
-      void* ail = ws + off_ail;
-      void* aiu = ws + off_aiu;
-      e = launch_isai(P->dp, nsys, lu, ail, aiu, fp32 ? 1 : 0, ft, st, o.reduction == BILU_REDUCE_FAST ? 1 : 0);
-      if (e != cudaSuccess) return cuda_err(e, "isai");
-      a.prec = PK_ISAI;
-      a.ail = ail;
-      a.aiu = aiu;
-    } else {
-      a.prec = PK_LU_GLOBAL;
-      if (fp32) {
-        float* f = (float*)(ws + off_f);
-        e = launch_to_float(lu, f, nz, st);
-        if (e != cudaSuccess) return cuda_err(e, "convert");
-        a.F = f;
+      double* lu = (double*)(ws + sc.lu);
+      if (prec == BILU_PRECOND_ILU0_SPLIT || prec == BILU_PRECOND_ILU0_ISAI)
+        e = launch_ilu0(P->dp, nsys, fv, lu, o.ilu_approach, ft, st);
+      else
+        e = launch_parilu0(P->dp, nsys, fv, lu_init, lu, o.parilu_sweeps, ft, st, o.parilu_res_tol,
+                           R ? R->parilu_sweeps : nullptr, R ? R->ilu_residual : nullptr,
+                           o.reduction == BILU_REDUCE_FAST ? 1 : 0);
+      if (e != cudaSuccess) return cuda_err(e, "factorisation");
+      if (is_isai(prec)) {
+        void* ail = ws + sc.ail;
+        void* aiu = ws + sc.aiu;
+        e = launch_isai(P->dp, nsys, lu, ail, aiu, fp32 ? 1 : 0, ft, st, o.reduction == BILU_REDUCE_FAST ? 1 : 0);
+        if (e != cudaSuccess) return cuda_err(e, "isai");
+        a.prec = PK_ISAI;
+        a.ail = ail;
+        a.aiu = aiu;
       } else {
-        a.F = lu;
+        a.prec = PK_LU_GLOBAL;
+        if (fp32) {
+          float* f = (float*)(ws + sc.f);
+          e = launch_to_float(lu, f, nz, st);
+          if (e != cudaSuccess) return cuda_err(e, "convert");
+          a.F = f;
+        } else {
+          a.F = lu;
+        }
       }
-    }
     }
   }
   int maxl = P->a_maxl;
@@ -1144,15 +1144,15 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
     }
   }
   if (P->timing) cudaEventRecord(P->ev[1], st);
-  if (sell_u) {
-    e = launch_to_sell(P->dp.su_src, P->dp.su_nnz, P->dp.aiu_nnz, nsys, a.aiu, ws + off_usell, fp32 ? 4 : 8, st);
+  if (sc.sell_u) {
+    e = launch_to_sell(P->dp.su_src, P->dp.su_nnz, P->dp.aiu_nnz, nsys, a.aiu, ws + sc.usell, fp32 ? 4 : 8, st);
     if (e != cudaSuccess) return cuda_err(e, "SELL copy of aiU");
-    a.aiu_sell = ws + off_usell;
+    a.aiu_sell = ws + sc.usell;
   }
-  if (sell_a) {
-    e = launch_to_sell(P->dp.sa_src, P->dp.sa_nnz, P->dp.a_nnz, nsys, vals, ws + off_asell, 8, st);
+  if (sc.sell_a) {
+    e = launch_to_sell(P->dp.sa_src, P->dp.sa_nnz, P->dp.a_nnz, nsys, vals, ws + sc.asell, 8, st);
     if (e != cudaSuccess) return cuda_err(e, "SELL copy of A");
-    a.A_sell = (const double*)(ws + off_asell);
+    a.A_sell = (const double*)(ws + sc.asell);
   }
   e = P->rr ? launch_solve_rr(a, P->rr_lay, P->rr_threads, P->rr_pv, fp32 ? 1 : 0,
                               o.reduction == BILU_REDUCE_FAST ? 0 : 1, P->rr_occ4 ? 1 : 0, st)
@@ -1160,6 +1160,34 @@ bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double*
   if (e != cudaSuccess) return cuda_err(e, "solver launch");
   if (P->timing) cudaEventRecord(P->ev[2], st);
   return BILU_OK;
+}
+
+}  // namespace bilu
+
+namespace plan_detail {
+
+// factor-pattern values for the factorisation kernels: the caller's array
+// when no diagonal was inserted, else an expanded copy in `scratch`
+const double* factor_values(bilu_plan* P, int nsys, const double* vin, double* scratch, cudaStream_t st,
+                            cudaError_t* err) {
+  *err = cudaSuccess;
+  if (P->missing == 0) return vin;
+  *err = launch_expand(P->dp, nsys, vin, scratch, st);
+  return scratch;
+}
+
+bilu_status solve_impl(bilu_plan* P, int nsys, const double* vals, const double* lu_init, const double* b, double* x,
+                       const bilu_results* R, cudaStream_t st) {
+  if (nsys < 0 || (nsys > 0 && (!vals || !b || !x))) return set_error(BILU_ERR_INVALID, "bilu_solve: bad arguments");
+  if (P->opts.isai_lower_diag)
+    return set_error(BILU_ERR_INVALID, "bilu_solve: plans with isai_lower_diag = 1 only serve bilu_isai");
+  if (nsys == 0) return BILU_OK;
+  const SolveScratch sc = solve_scratch_layout(P, nsys);
+  if (sc.total > 0) {
+    bilu_status s = ensure_ws(P, sc.total);
+    if (s) return s;
+  }
+  return solve_launch(P, nsys, vals, lu_init, b, x, R, static_cast<char*>(P->ws), sc, st);
 }
 
 }  // namespace plan_detail

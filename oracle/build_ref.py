@@ -6,7 +6,8 @@ Test infrastructure only.  Two outputs, both in the git-ignored oracle/_ref/:
 
 1. Where the reference sources are present (this build container), each
    reference translation unit on the solver path is compiled for sm_103a into
-   a cubin, straight from the files under /root/reference.  A generated
+   a cubin, straight from the files of the reference checkout (the directory
+   named by MERGING_ILU0_REFERENCE, default /root/reference).  A generated
    wrapper unit includes the reference's header.h first and raises its
    compile-time capacity limits (MAX_NUM_ROWS 54 -> 512, MAX_NUM_NZ 2560 kept),
    then includes the reference .cu unchanged; header.h's `#pragma once` keeps
@@ -26,7 +27,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF = "/root/reference/Batched-ILU0-merged/ILU0_ISAI_bicgstab"
+# the reference checkout: MERGING_ILU0_REFERENCE names its root (default /root/reference)
+REF_ROOT = os.environ.get("MERGING_ILU0_REFERENCE", "/root/reference")
+REF = os.path.join(REF_ROOT, "Batched-ILU0-merged", "ILU0_ISAI_bicgstab")
 
 # (cubin name, reference translation unit)
 UNITS = [

@@ -91,6 +91,36 @@ def oracle_pipeline(rp, ci, vals, b, precond, approach=1, sweeps=5, fp32=False, 
     return out
 
 
+def oracle_fast(rp, ci, v, b, precond, nt, fp32, approach=3, sweeps=5, power=2, **tol):
+    """The oracle's restatement of the FAST order (orc_bicgstab_fast) for one preconditioner family with `nt`
+    threads per system: factors, ISAI values and the solve, as the register-resident kernel computes them."""
+    nrp, nci, src = O.add_missing_diag(rp, ci)
+    fv = np.where(src[None, :] >= 0, v[:, np.maximum(src, 0)], 0.0)
+    if precond == bilu.PRECOND_NONE:
+        return O.bicgstab_fast(rp, ci, v, b, nt, pv=0, **tol)
+    if precond == bilu.PRECOND_GENERAL_ISAI:
+        arp, aci = O.isai_pattern(nrp, nci, power)
+        ai = O.isai_values(nrp, nci, fv, 2, arp, aci)
+        return O.bicgstab_fast(rp, ci, v, b, nt, pv=2, ail=(arp, aci, ai), fp32=fp32, **tol)
+    if precond in (bilu.PRECOND_ILU0, bilu.PRECOND_ILU0_SPLIT, bilu.PRECOND_PARILU0):
+        if precond == bilu.PRECOND_PARILU0:
+            lu = O.parilu0(nrp, nci, fv, sweeps, fast=True)
+        else:
+            lu = O.ilu0(nrp, nci, fv, approach)
+        return O.bicgstab_fast(rp, ci, v, b, nt, pv=3, ail=(nrp, nci, lu), fp32=fp32, **tol)
+    if precond == bilu.PRECOND_ILU0_ISAI:
+        lu = O.ilu0(nrp, nci, fv, approach)
+    else:
+        lu = O.parilu0(nrp, nci, fv, sweeps, fast=True)
+    lrp, lci, urp, uci = O.split_pattern(nrp, nci)
+    Lv, Uv = O.split_values(nrp, nci, lu)
+    arp, aci = O.isai_pattern(lrp, lci, power)
+    brp, bci = O.isai_pattern(urp, uci, power)
+    ail = O.isai_values(lrp, lci, Lv, 0, arp, aci, fast=2 if fp32 else False)
+    aiu = O.isai_values(urp, uci, Uv, 1, brp, bci, fast=2 if fp32 else True)
+    return O.bicgstab_fast(rp, ci, v, b, nt, pv=1, ail=(arp, aci, ail), aiu=(brp, bci, aiu), fp32=fp32, **tol)
+
+
 def gpu_solve(dev, rp, ci, vals, b, lu_init=None, **opts):
     """Solve through the C ABI; returns numpy results and the plan info."""
     import torch

@@ -17,32 +17,7 @@ NSYS = 10
 TOL = dict(tol_mode=bilu.TOL_REL, tol=1e-10)
 
 
-def _oracle_fast(rp, ci, v, b, precond, nt, fp32, approach=3, sweeps=5, power=2, **tol):
-    nrp, nci, src = O.add_missing_diag(rp, ci)
-    fv = np.where(src[None, :] >= 0, v[:, np.maximum(src, 0)], 0.0)
-    if precond == bilu.PRECOND_NONE:
-        return O.bicgstab_fast(rp, ci, v, b, nt, pv=0, **tol)
-    if precond == bilu.PRECOND_GENERAL_ISAI:
-        arp, aci = O.isai_pattern(nrp, nci, power)
-        ai = O.isai_values(nrp, nci, fv, 2, arp, aci)
-        return O.bicgstab_fast(rp, ci, v, b, nt, pv=2, ail=(arp, aci, ai), fp32=fp32, **tol)
-    if precond in (bilu.PRECOND_ILU0, bilu.PRECOND_ILU0_SPLIT, bilu.PRECOND_PARILU0):
-        if precond == bilu.PRECOND_PARILU0:
-            lu = O.parilu0(nrp, nci, fv, sweeps, fast=True)
-        else:
-            lu = O.ilu0(nrp, nci, fv, approach)
-        return O.bicgstab_fast(rp, ci, v, b, nt, pv=3, ail=(nrp, nci, lu), fp32=fp32, **tol)
-    if precond == bilu.PRECOND_ILU0_ISAI:
-        lu = O.ilu0(nrp, nci, fv, approach)
-    else:
-        lu = O.parilu0(nrp, nci, fv, sweeps, fast=True)
-    lrp, lci, urp, uci = O.split_pattern(nrp, nci)
-    Lv, Uv = O.split_values(nrp, nci, lu)
-    arp, aci = O.isai_pattern(lrp, lci, power)
-    brp, bci = O.isai_pattern(urp, uci, power)
-    ail = O.isai_values(lrp, lci, Lv, 0, arp, aci, fast=2 if fp32 else False)
-    aiu = O.isai_values(urp, uci, Uv, 1, brp, bci, fast=2 if fp32 else True)
-    return O.bicgstab_fast(rp, ci, v, b, nt, pv=1, ail=(arp, aci, ail), aiu=(brp, bci, aiu), fp32=fp32, **tol)
+_oracle_fast = H.oracle_fast
 
 
 def _check(g, o, what, fields=("iters", "conv", "status", "res", "x", "true_res")):
@@ -86,6 +61,70 @@ def test_rr_large_system_eight_rows_per_thread(cuda):
     assert g["info"]["threads"] == 128
     o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_PARILU0_ISAI, 128, True, **TOL)
     _check(g, o, "3D 10x10x10 ParILU+ISAI FP32")
+
+
+HEADLINE_OPTS = dict(precond=bilu.PRECOND_PARILU0_ISAI, parilu_sweeps=5, isai_power=2, reduction=bilu.REDUCE_FAST,
+                     factor_precision=bilu.FP32, max_iter=500, **TOL)
+
+
+@pytest.mark.parametrize("staging", [16, 6, 0])
+def test_headline_configuration_bitwise(cuda, staging):
+    """The benchmark's headline path (PrecondBiCGSTAB_ilu_isai_gpu.cu:267-339: ParILU, ISAI of L and U, solver)
+    on 16 systems of its 3D 7-point 10x10x10 pattern: ParILU(0) 5 sweeps (k_parilu0, FAST), ISAI computed in
+    FP32 (k_isai_f32), 128 threads with 8 rows each.  Staging 16 is the configuration the autotuner picks for
+    the 4096-system headline on GB300: the 4-CTA-per-SM kernel (k_bicgstab_rr_occ4, 128 registers, four
+    block reductions of 4 warps) with every operand read through L1; 6 stages aiL and aiU in shared memory
+    (3 CTAs per SM), 0 stages nothing.  x, iterations, status, both norms and the true residual equal the
+    oracle's FAST order bit for bit."""
+    rp, ci, v, b = H.workload("3d7_10x10x10", 16)
+    g = H.gpu_solve(cuda, rp, ci, v, b, smem_staging=staging, threads_per_system=128, **HEADLINE_OPTS)
+    info = g["info"]
+    assert info["threads"] == 128
+    assert bool(info["operands_in_smem"] & 16) == (staging == 16), info
+    o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_PARILU0_ISAI, 128, True, **TOL)
+    _check(g, o, f"headline 3D 10x10x10 ParILU(5)+FP32 ISAI, staging {staging}")
+    assert np.all(g["conv"] == 1) and np.all(g["status"] == bilu.SYS_CONVERGED)
+
+
+def test_headline_autotuned_plan_bitwise(cuda):
+    """The headline plan as the benchmark uses it: bilu_plan_autotune on the batch, then solves with the same
+    plan (whatever thread count, staging, SELL-32 copies or kernel variant it kept) equal the oracle."""
+    import torch
+    rp, ci, v, b = H.workload("3d7_10x10x10", 24)
+    with bilu.Plan(rp, ci, **HEADLINE_OPTS) as plan:
+        V = torch.from_numpy(v).to(cuda)
+        B = torch.from_numpy(b).to(cuda)
+        X = torch.empty_like(B)
+        info = plan.autotune(V, B, X)
+        assert info["solver_kernel"] == 1
+        nsys, n = b.shape
+        out = dict(x=torch.full_like(B, float("nan")), iters=torch.full((nsys,), -7.0, device=cuda),
+                   conv=torch.full((nsys,), 7, dtype=torch.int32, device=cuda),
+                   res=torch.full((nsys,), -1.0, dtype=torch.float64, device=cuda),
+                   true_res=torch.full((nsys,), -1.0, dtype=torch.float64, device=cuda),
+                   status=torch.full((nsys,), 99, dtype=torch.int32, device=cuda))
+        plan.solve(V, B, out["x"], out["iters"], out["conv"], out["res"], out["true_res"], out["status"])
+        torch.cuda.synchronize()
+        g = {k: t.cpu().numpy() for k, t in out.items()}
+        g["info"] = plan.info()
+    o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_PARILU0_ISAI, info["threads"], True, **TOL)
+    _check(g, o, f"autotuned headline plan (threads {info['threads']}, staging {info['operands_in_smem']})")
+
+
+@pytest.mark.parametrize("nt,staging", [(96, 16), (96, 6), (192, -1), (384, -1)])
+def test_cd2d_24x24_fp32_isai_bitwise(cuda, nt, staging):
+    """The precision-variant workload: 2D 5-point 24x24 convection-diffusion (n = 576), ILU(0) approach 3 +
+    ISAI of L and U computed, stored and applied in FP32, FAST order, at the autotuner's thread counts (96
+    threads with 8 rows each, on the 4-CTA kernel or with the ISAI values staged; 192 and 384 threads)."""
+    rp, ci, v, b = H.workload("cd2d_24x24", 8)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=bilu.PRECOND_ILU0_ISAI, ilu_approach=3, reduction=bilu.REDUCE_FAST,
+                    factor_precision=bilu.FP32, threads_per_system=nt, smem_staging=staging, **TOL)
+    assert g["info"]["threads"] == nt
+    if staging == 16:
+        assert g["info"]["operands_in_smem"] & 16
+    o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_ILU0_ISAI, nt, True, approach=3, **TOL)
+    _check(g, o, f"cd2d 24x24 ILU(0)+FP32 ISAI, {nt} threads, staging {staging}")
+    assert np.all(g["conv"] == 1)
 
 
 def test_rr_edge_cases(cuda):

@@ -25,7 +25,9 @@ PKG = os.path.join(ROOT, "merging-ilu0_gb300")
 SHIM_INC = os.path.join(PKG, "shim", "include")
 SHIM_LIB = os.path.join(PKG, "libbilu_ref.so")
 DRIVER_SRC = os.path.join(ROOT, "tests", "shim_driver.cpp")
-REF_DIR = "/root/reference/Batched-ILU0-merged/ILU0_ISAI_bicgstab"
+# the reference checkout: MERGING_ILU0_REFERENCE names its root (default /root/reference)
+REF_DIR = os.path.join(os.environ.get("MERGING_ILU0_REFERENCE", "/root/reference"), "Batched-ILU0-merged",
+                       "ILU0_ISAI_bicgstab")
 DRIVERS = ["main_bicgstab_ilu", "main_bicgstab_ilu_merged", "main_bicgstab_ilu_segregated",
            "main_bicgstab_ilu_isai", "main_bicgstab_general_isai"]
 
