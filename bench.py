@@ -685,7 +685,7 @@ def main():
     if rank != 0:
         return
     # FP64 FMA issue rate of this GPU, measured now (bilu_probe_fp64_rate): the FP64 roofline's peak
-    fp64_peak = bilu.probe_fp64_rate()
+    fp64_peak, fp64_probe_mhz = bilu.probe_fp64_rate()
     chosen = {}
     by_name = {sc.get("name"): sc for sc in secondary if "systems_per_s" in sc}
     plain = by_name.get("plain_ilu0_3d7_10x10x10")
@@ -773,7 +773,8 @@ def main():
         "roofline_fp64": {"achieved": flops / solve_s / 1e9, "peak": fp64_peak, "unit": "GFLOP/s",
                           "frac": flops / solve_s / 1e9 / fp64_peak,
                           "peak_kind": "measured in this run: bilu_probe_fp64_rate (independent DFMA chains on every "
-                                       "SM, CUDA events, best of 5 launches)",
+                                       "SM, CUDA events, best of 3 launch shapes x 5 launches)",
+                          "peak_sm_mhz": fp64_probe_mhz,
                           "counted": "FP64 operations of the BiCGSTAB iterations (bench.fp64_flops_per_iter x mean "
                                      "iterations x systems); FP32 ISAI work not counted",
                           "ncu": RR_NCU if autotuned_occ4 else None,

@@ -382,10 +382,12 @@ const char* bilu_version(void);
 /* Number of CUDA devices visible (0 when none; never fails). */
 int bilu_device_count(void);
 /* FP64 FMA throughput of the current device in GFLOP/s (two FLOPs per FMA),
- * measured with CUDA events on independent DFMA chains that fill every SM:
- * the peak against which the FP64 roofline of the solver kernels is quoted.
- * Synchronises the stream.  No reference counterpart. */
-bilu_status bilu_probe_fp64_rate(double* h_gflops, void* stream);
+ * measured with CUDA events on independent DFMA chains that fill every SM
+ * (the best of three launch shapes): the peak against which the FP64 roofline
+ * of the solver kernels is quoted.  h_sm_mhz (optional) receives the SM clock
+ * during the best launch, from the SM cycle counter and the global timer.
+ * Allocates 32 bytes and synchronises the stream.  No reference counterpart. */
+bilu_status bilu_probe_fp64_rate(double* h_gflops, double* h_sm_mhz, void* stream);
 
 /* ---------------------------------------------------------------- synthetic inputs */
 /* Seeded generators of the benchmark workloads (host memory; no GPU needed).

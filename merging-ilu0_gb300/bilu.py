@@ -119,7 +119,7 @@ def lib():
         L.bilu_mlp_warm_start.argtypes = [vp, vp, i, vp, vp, d, vp, vp, vp]
         L.bilu_mlp_save.argtypes = [vp, C.c_char_p]
         L.bilu_mlp_load.argtypes = [vp, C.c_char_p]
-        L.bilu_probe_fp64_rate.argtypes = [C.POINTER(d), vp]
+        L.bilu_probe_fp64_rate.argtypes = [C.POINTER(d), C.POINTER(d), vp]
         L.bilu_plan_enable_timing.argtypes = [vp, i]
         L.bilu_plan_last_timing.argtypes = [vp, C.POINTER(Timing)]
         L.bilu_gen_uneven.argtypes = [i, C.c_uint64, i, i, i, i, ip, ip, ip, ip, C.POINTER(d), C.POINTER(d)]
@@ -172,10 +172,11 @@ def version():
 
 
 def probe_fp64_rate(stream=None):
-    """FP64 FMA throughput of the current device, GFLOP/s (bilu_probe_fp64_rate)."""
-    g = C.c_double()
-    _check(lib().bilu_probe_fp64_rate(C.byref(g), _stream(stream)))
-    return g.value
+    """(FP64 FMA throughput of the current device in GFLOP/s, SM clock during the measurement in MHz);
+    bilu_probe_fp64_rate."""
+    g, m = C.c_double(), C.c_double()
+    _check(lib().bilu_probe_fp64_rate(C.byref(g), C.byref(m), _stream(stream)))
+    return g.value, m.value
 
 
 # ---------------------------------------------------------------- generators

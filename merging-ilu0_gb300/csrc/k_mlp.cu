@@ -2,9 +2,10 @@
 // its tanh form, BF16 weights, FP32 accumulation) that predicts the converged
 // ParILU factors, trained on the GPU by these kernels.  No counterpart in the
 // reference.  Training runs on CUDA cores with an accurate tanh; inference
-// (k_mlp_warm) runs the 64x64 layer on the tensor cores (mma.sync BF16 with
-// FP32 accumulation, activations split into BF16 high + low parts so the
-// products keep FP32-level precision) and the hardware tanh approximation.
+// (k_mlp_warm) runs the 64x64 layer on the Blackwell tensor cores (tcgen05.mma
+// with BF16 operands in shared memory and FP32 accumulators in tensor memory,
+// activations split into BF16 high + low parts so the products keep
+// FP32-level precision) and the hardware tanh approximation.
 //
 // Features of nonzero (i, j) of system s, all scaled by d = |a_ii|:
 //   a_ij, a_ii, a_jj, ||A(i,:)||_2, ||A(:,j)||_2 (column over the structurally
@@ -21,6 +22,7 @@
 #include <cstdint>
 
 #include "bilu_internal.h"
+#include "k_tc.cuh"
 
 namespace bilu {
 namespace {
@@ -323,38 +325,29 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
   return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// d += a * b, m16n8k16, BF16 operands, FP32 accumulators
-__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-// Warm start: persistent CTAs over the systems (the network's weights are
-// staged once per CTA).  Entries with no dependency pairs on or above the
-// diagonal converge to a_ij exactly and are copied.  The others go through the
-// network in tiles of 32 per warp: every lane forms one entry's features, then
-// each 16-entry half runs as m16n8k16 MMAs -- every lane forms the first-layer
-// activations it needs for its A fragments (rows g and g+8, k = 2t, 2t+1,
-// 2t+8, 2t+9 of each 16-wide chunk; g = lane/4, t = lane%4), split into BF16
-// high and low parts; layer 2 is 2 x 4 x 8 MMAs against W2 (BF16); GELU and
-// the output layer reduce over the 4 lanes of a quad.  The ILU residual
-// ||(A - L0 U0)|_S||_F / ||A||_F then decides between the prediction and the
-// plain initialisation lu0 = A.
-//
-// Shared-memory weight layout, arranged so that each lane fetches its operands
-// with 128-bit loads (the kernel is bound by shared-memory traffic otherwise):
-//   w1p [64][12]     hidden unit v: W1[v][0..8], b1[v], 0, 0
-//   bw  [8][4] x 4   slice ut, quad index t: b2[u], b2[u+1], w3[u], w3[u+1], u = 8 ut + 2 t
-//   b3  [4]          b3, 0, 0, 0
-//   w2f [8][32][8]   slice ut, lane: its B fragments of the 4 k-chunks, (W2 row 8 ut + g,
-//                    words 8 ch + t and 8 ch + 4 + t) for ch = 0..3
-constexpr int WARM_THREADS = 256;
-constexpr int WP_W1 = 0, WP_BW = H * 12, WP_B3 = WP_BW + 8 * 4 * 4, WP_W2 = WP_B3 + 4;
-constexpr int WP_WORDS = WP_W2 + 8 * 32 * 8;
-static_assert(WP_W2 % 4 == 0 && WP_WORDS % 4 == 0, "16-byte aligned weight blocks");
+// Warm start: persistent CTAs of 128 threads over the systems (the network's
+// weights are staged once per CTA).  Entries with no dependency pairs on or
+// above the diagonal converge to a_ij exactly and are copied.  The others go
+// through the network in tiles of 128, one entry per thread:
+//   layer 1 (9 -> 64) on the CUDA cores, GELU, the activations split into BF16
+//   high and low parts (h = hi + lo to about 16 bits) and stored as the two
+//   128 x 64 A operands of the tensor core (K-major, k_tc.cuh layout);
+//   layer 2 (64 x 64) as 8 tcgen05.mma of M = 128, N = 64, K = 16 (hi and lo
+//   against W2 in BF16, FP32 accumulation in 64 TMEM columns), issued by one
+//   thread and completed through an mbarrier;
+//   every thread reads its own row of the accumulator (tcgen05.ld, lane = row),
+//   adds b2, GELU, and the output layer's dot product with w3.
+// The ILU residual ||(A - L0 U0)|_S||_F / ||A||_F then decides between the
+// prediction and the plain initialisation lu0 = A.
+// The mbarrier waits are bounded: a CTA whose tensor-core work does not
+// complete in time stops using it and writes the plain initialisation
+// (used = 0, ILU residual -1) for its remaining systems.
+constexpr int WARM_THREADS = 128;
+constexpr int WT_AH = 0, WT_AL = WT_AH + 128 * H * 2, WT_B = WT_AL + 128 * H * 2, WT_W1 = WT_B + H * H * 2;
+constexpr int WT_BW = WT_W1 + H * 12 * 4, WT_LU = WT_BW + H * 8;
+constexpr uint32_t kTmemCols = 64;
+constexpr uint32_t kWaitLimit = 1u << 24;
+static_assert(WT_W1 % 16 == 0 && WT_LU % 16 == 0, "aligned operand blocks");
 
 __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, int nsys,
                                                            const double* __restrict__ A,
@@ -364,43 +357,57 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
                                                            const __nv_bfloat16* __restrict__ pbf, double threshold,
                                                            double* __restrict__ LU0, double* __restrict__ res_out,
                                                            int* __restrict__ used) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  float* wp = reinterpret_cast<float*>(smraw);
-  uint32_t* w2f = reinterpret_cast<uint32_t*>(wp + WP_W2);
-  double* lu = reinterpret_cast<double*>(wp + WP_WORDS);
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  __shared__ uint64_t s_mbar;
+  __shared__ uint32_t s_tmem;
   __shared__ double s_num[WARM_THREADS / 32], s_den[WARM_THREADS / 32];
-  __shared__ int s_ok;
-  for (int k = threadIdx.x; k < H * 12; k += blockDim.x) {
-    const int v = k / 12, c = k % 12;
-    wp[WP_W1 + k] = c < NF ? __bfloat162float(pbf[OW1 + v * NF + c]) : (c == NF ? __bfloat162float(pbf[OB1 + v]) : 0.0f);
+  __shared__ int s_ok, s_fail;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // weights: W2 as the K-major B operand (row u = output unit, k = input unit), W1 / b1 as float4 x 3 per
+  // hidden unit, (b2, w3) pairs
+  {
+    const uint4* w2g = reinterpret_cast<const uint4*>(pbf + OW2);  // row u: 8 chunks of 8 BF16
+    for (int k = tid; k < H * 8; k += WARM_THREADS) {
+      const int u = k >> 3, c = k & 7;
+      *reinterpret_cast<uint4*>(smraw + WT_B + tc::kmajor_off(u, 8 * c, H)) = w2g[k];
+    }
+    float* w1 = reinterpret_cast<float*>(smraw + WT_W1);
+    for (int k = tid; k < H * 12; k += WARM_THREADS) {
+      const int v = k / 12, c = k % 12;
+      w1[k] = c < NF ? __bfloat162float(pbf[OW1 + v * NF + c]) : (c == NF ? __bfloat162float(pbf[OB1 + v]) : 0.0f);
+    }
+    float2* bw = reinterpret_cast<float2*>(smraw + WT_BW);
+    for (int u = tid; u < H; u += WARM_THREADS) bw[u] = make_float2(__bfloat162float(pbf[OB2 + u]), __bfloat162float(pbf[OW3 + u]));
   }
-  for (int k = threadIdx.x; k < 8 * 4 * 4; k += blockDim.x) {
-    const int ut = k >> 4, t = (k >> 2) & 3, c = k & 3, u = ut * 8 + 2 * t + (c & 1);
-    wp[WP_BW + k] = __bfloat162float(pbf[(c < 2 ? OB2 : OW3) + u]);
+  if (tid == 0) {
+    tc::mbar_init(&s_mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_fail = 0;
   }
-  if (threadIdx.x < 4) wp[WP_B3 + threadIdx.x] = threadIdx.x == 0 ? __bfloat162float(pbf[OB3]) : 0.0f;
-  const uint32_t* w2g = reinterpret_cast<const uint32_t*>(pbf + OW2);  // row u: 32 words of 2 BF16
-  for (int k = threadIdx.x; k < 8 * 32 * 8; k += blockDim.x) {
-    const int ut = k >> 8, ln = (k >> 3) & 31, c = k & 7, ch = c >> 1;
-    const int g = ln >> 2, t = ln & 3;
-    w2f[k] = w2g[(ut * 8 + g) * (H / 2) + ch * 8 + (c & 1) * 4 + t];
-  }
-  __syncthreads();  // staged weights visible to every warp before b3 is read below
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  const int g = lane >> 2, t = lane & 3;
-  const float4* w1v = reinterpret_cast<const float4*>(wp + WP_W1);
-  const float4* bwv = reinterpret_cast<const float4*>(wp + WP_BW);
-  const uint4* w2v = reinterpret_cast<const uint4*>(w2f);
-  const float b3 = wp[WP_B3];
-  const int ntile = (P.n_mlp + 31) >> 5;
+  if (warp == 0) tc::alloc(&s_tmem, kTmemCols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  const float4* w1v = reinterpret_cast<const float4*>(smraw + WT_W1);
+  const float2* bw = reinterpret_cast<const float2*>(smraw + WT_BW);
+  const float b3 = __bfloat162float(pbf[OB3]);
+  double* lu = reinterpret_cast<double*>(smraw + WT_LU);
+  const uint32_t a_hi = tc::smem_u32(smraw + WT_AH), a_lo = tc::smem_u32(smraw + WT_AL);
+  const uint32_t b_w2 = tc::smem_u32(smraw + WT_B);
+  constexpr uint32_t kSbo = H * 16;  // K = 64: 8-row groups 1024 bytes apart
+  const uint32_t idesc = tc::idesc_bf16(128, H);
+  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's 32 TMEM lanes
+  const int ntile = (P.n_mlp + WARM_THREADS - 1) / WARM_THREADS;
+  uint32_t phase = 0;
   for (int s = blockIdx.x; s < nsys; s += gridDim.x) {
     __syncthreads();  // the previous system's lu and s_ok no longer read
     const double* As = A + (size_t)s * P.nnz;
-    for (int e = threadIdx.x; e < P.nnz; e += blockDim.x) lu[e] = As[e];  // exact for the copied entries
+    for (int e = tid; e < P.nnz; e += WARM_THREADS) lu[e] = As[e];  // exact for the copied entries
+    const bool failed = s_fail != 0;  // uniform: written before the last barrier
     __syncthreads();
-    for (int tile = warp; tile < ntile; tile += nwarp) {
-      // features of entry tile*32 + lane
-      const int q = tile * 32 + lane;
+    for (int tile = 0; tile < ntile && !failed; ++tile) {
+      const int q = tile * WARM_THREADS + tid;
       const bool live = q < P.n_mlp;
       float f[NF];
       double ab = 0.0;
@@ -415,95 +422,85 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
 #pragma unroll
         for (int k = 0; k < NF; ++k) f[k] = 0.0f;
       }
+      // layer 1 on the CUDA cores, 8 hidden units at a time into one 16-byte chunk of each A operand
 #pragma unroll 1
-      for (int half = 0; half < 2; ++half) {
-        float xa[NF], xb[NF];  // rows g and g+8 of this half
+      for (int c = 0; c < H / 8; ++c) {
+        uint32_t hi[4], lo[4];
 #pragma unroll
-        for (int k = 0; k < NF; ++k) {
-          xa[k] = __shfl_sync(kFull, f[k], 16 * half + g);
-          xb[k] = __shfl_sync(kFull, f[k], 16 * half + g + 8);
-        }
-        // first layer on CUDA cores, straight into A fragments (high and low parts)
-        uint32_t ahi[4][4], alo[4][4];
+        for (int d = 0; d < 8; d += 2) {
+          float h2[2];
 #pragma unroll
-        for (int ch = 0; ch < 4; ++ch) {
+          for (int x = 0; x < 2; ++x) {
+            const int v = 8 * c + d + x;
+            const float4 wa = w1v[v * 3], wb = w1v[v * 3 + 1], wc = w1v[v * 3 + 2];
+            const float w[NF] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w, wc.x};
+            float pa = wc.y;  // b1
 #pragma unroll
-          for (int hh = 0; hh < 2; ++hh) {  // k = 2t, 2t+1 (hh 0) and 2t+8, 2t+9 (hh 1)
-            const int v0 = ch * 16 + 2 * t + 8 * hh;
-            float ha[2], hb[2];
-#pragma unroll
-            for (int d = 0; d < 2; ++d) {
-              const float4 wa = w1v[(v0 + d) * 3], wb = w1v[(v0 + d) * 3 + 1], wc = w1v[(v0 + d) * 3 + 2];
-              const float w[NF] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w, wc.x};
-              float pa = wc.y, pb = wc.y;  // b1
-#pragma unroll
-              for (int k = 0; k < NF; ++k) {
-                pa = fmaf(w[k], xa[k], pa);
-                pb = fmaf(w[k], xb[k], pb);
-              }
-              ha[d] = gelu_fast(pa);
-              hb[d] = gelu_fast(pb);
-            }
-            const float ha0h = __bfloat162float(__float2bfloat16_rn(ha[0]));
-            const float ha1h = __bfloat162float(__float2bfloat16_rn(ha[1]));
-            const float hb0h = __bfloat162float(__float2bfloat16_rn(hb[0]));
-            const float hb1h = __bfloat162float(__float2bfloat16_rn(hb[1]));
-            ahi[ch][2 * hh + 0] = pack_bf16(ha0h, ha1h);
-            ahi[ch][2 * hh + 1] = pack_bf16(hb0h, hb1h);
-            alo[ch][2 * hh + 0] = pack_bf16(ha[0] - ha0h, ha[1] - ha1h);
-            alo[ch][2 * hh + 1] = pack_bf16(hb[0] - hb0h, hb[1] - hb1h);
+            for (int k = 0; k < NF; ++k) pa = fmaf(w[k], f[k], pa);
+            h2[x] = gelu_fast(pa);
           }
+          const float h0 = __bfloat162float(__float2bfloat16_rn(h2[0]));
+          const float h1 = __bfloat162float(__float2bfloat16_rn(h2[1]));
+          hi[d >> 1] = pack_bf16(h0, h1);
+          lo[d >> 1] = pack_bf16(h2[0] - h0, h2[1] - h1);
         }
-        // register order of the A fragment: a0 (row g, k 2t..), a1 (row g+8, k 2t..), a2 (row g, k 2t+8..),
-        // a3 (row g+8, k 2t+8..)
-        float outa = 0.0f, outb = 0.0f;
+        const uint32_t off = tc::kmajor_off(tid, 8 * c, H);
+        *reinterpret_cast<uint4*>(smraw + WT_AH + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4*>(smraw + WT_AL + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      }
+      // the operands (generic-proxy stores) become visible to the tensor core, and every thread's
+      // previous accumulator reads are done, before one thread issues layer 2
+      tc::fence_smem_to_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
 #pragma unroll
-        for (int ut = 0; ut < 8; ++ut) {
-          float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-          const uint4 q0 = w2v[(ut * 32 + lane) * 2], q1 = w2v[(ut * 32 + lane) * 2 + 1];
-          const uint32_t bfr[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+        for (int j = 0; j < H / 16; ++j)
+          tc::mma_bf16(tmem, tc::sdesc(a_hi + 256 * j, kSbo), tc::sdesc(b_w2 + 256 * j, kSbo), idesc, j > 0);
 #pragma unroll
-          for (int ch = 0; ch < 4; ++ch) {
-            const uint32_t ah[4] = {ahi[ch][0], ahi[ch][1], ahi[ch][2], ahi[ch][3]};
-            const uint32_t al[4] = {alo[ch][0], alo[ch][1], alo[ch][2], alo[ch][3]};
-            mma_bf16(c, ah, bfr[2 * ch], bfr[2 * ch + 1]);
-            mma_bf16(c, al, bfr[2 * ch], bfr[2 * ch + 1]);
-          }
-          const float4 bw = bwv[ut * 4 + t];  // b2[u], b2[u+1], w3[u], w3[u+1]
-          outa = fmaf(bw.z, gelu_fast(c[0] + bw.x), outa);
-          outa = fmaf(bw.w, gelu_fast(c[1] + bw.y), outa);
-          outb = fmaf(bw.z, gelu_fast(c[2] + bw.x), outb);
-          outb = fmaf(bw.w, gelu_fast(c[3] + bw.y), outb);
-        }
-        outa += __shfl_xor_sync(kFull, outa, 1);
-        outa += __shfl_xor_sync(kFull, outa, 2);
-        outb += __shfl_xor_sync(kFull, outb, 1);
-        outb += __shfl_xor_sync(kFull, outb, 2);
-        // the entry of row r (0..15) of this half lives on lane 16*half + r; rows r < 8
-        // were reduced on lane 4r (outa), rows 8..15 on lane 4(r-8) (outb)
-        const int r = lane & 15;
-        const float ya = __shfl_sync(kFull, outa, (r & 7) << 2);
-        const float yb = __shfl_sync(kFull, outb, (r & 7) << 2);
-        if (live && (lane >> 4) == half) {
-          const float y = (r < 8 ? ya : yb) + b3;
-          lu[e] = ab * (1.0 + (double)y);
+        for (int j = 0; j < H / 16; ++j)
+          tc::mma_bf16(tmem, tc::sdesc(a_lo + 256 * j, kSbo), tc::sdesc(b_w2 + 256 * j, kSbo), idesc, 1);
+        tc::commit(&s_mbar);
+      }
+      const bool done = tc::mbar_wait(&s_mbar, phase, kWaitLimit);
+      phase ^= 1u;
+      if (!done) s_fail = 1;
+      tc::fence_after_sync();
+      __syncthreads();
+      if (s_fail) break;  // uniform
+      // this thread's row of the accumulator: b2, GELU, output layer
+      float out = 0.0f;
+#pragma unroll 1
+      for (int c = 0; c < H / 16; ++c) {
+        float acc[16];
+        tc::ld16(trow + 16 * c, acc);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const float2 q2 = bw[16 * c + k];
+          out = fmaf(q2.y, gelu_fast(acc[k] + q2.x), out);
         }
       }
+      if (live) lu[e] = ab * (1.0 + (double)(out + b3));
+      tc::fence_before_sync();
     }
     __syncthreads();
+    const bool fail = s_fail != 0;
     // residual of the warm start: (A - LU)_ij = a_ij - sum_{k<min(i,j)} l_ik u_kj - (l_ij u_jj | u_ij)
     double num = 0.0, den = 0.0;
-    for (int e = threadIdx.x; e < P.nnz; e += blockDim.x) {
-      const int i = P.row_of[e], j = P.ci[e];
-      double acc = 0.0;
-      for (int q = P.dep_ptr[e]; q < P.dep_ptr[e + 1]; ++q) {
-        const int2 d = P.dep[q];
-        acc = fma(lu[d.x], lu[d.y], acc);
+    if (!fail) {
+      for (int e = tid; e < P.nnz; e += WARM_THREADS) {
+        const int i = P.row_of[e], j = P.ci[e];
+        double acc = 0.0;
+        for (int q = P.dep_ptr[e]; q < P.dep_ptr[e + 1]; ++q) {
+          const int2 d = P.dep[q];
+          acc = fma(lu[d.x], lu[d.y], acc);
+        }
+        acc = (j < i) ? fma(lu[e], lu[P.diag[j]], acc) : acc + lu[e];
+        const double rr = As[e] - acc;
+        num = fma(rr, rr, num);
+        den = fma(As[e], As[e], den);
       }
-      acc = (j < i) ? fma(lu[e], lu[P.diag[j]], acc) : acc + lu[e];
-      const double rr = As[e] - acc;
-      num = fma(rr, rr, num);
-      den = fma(As[e], As[e], den);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -515,21 +512,28 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
       s_den[warp] = den;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
       double a = 0.0, b = 0.0;
-      for (int w = 0; w < nwarp; ++w) {
+      for (int w = 0; w < WARM_THREADS / 32; ++w) {
         a += s_num[w];
         b += s_den[w];
       }
-      const double res = b > 0.0 ? sqrt(a / b) : sqrt(a);
-      s_ok = (res <= threshold) ? 1 : 0;  // NaN fails the test: fallback
+      const double res = fail ? -1.0 : (b > 0.0 ? sqrt(a / b) : sqrt(a));
+      s_ok = (!fail && res <= threshold) ? 1 : 0;  // NaN fails the test: fallback
       if (res_out) res_out[s] = res;
       if (used) used[s] = s_ok;
     }
     __syncthreads();
     const int ok = s_ok;
-    for (int e = threadIdx.x; e < P.nnz; e += blockDim.x) LU0[(size_t)s * P.nnz + e] = ok ? lu[e] : As[e];
+    for (int e = tid; e < P.nnz; e += WARM_THREADS) LU0[(size_t)s * P.nnz + e] = ok ? lu[e] : As[e];
   }
+  // a tensor-core round that timed out may still be in flight: wait for it once more (bounded) before the
+  // accumulator columns are freed
+  if (s_fail) tc::mbar_wait(&s_mbar, phase ^ 1u, kWaitLimit);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::dealloc(tmem, kTmemCols);
 }
 
 }  // namespace
@@ -585,7 +589,7 @@ cudaError_t launch_mlp_warm(const DevPattern& p, int nsys, const double* A, cons
                             const float* corr, const void* pbf, double threshold, double* lu0, double* res, int* used,
                             cudaStream_t st) {
   if (nsys == 0) return cudaSuccess;
-  const size_t smem = sizeof(float) * WP_WORDS + sizeof(double) * p.nnz;
+  const size_t smem = WT_LU + sizeof(double) * p.nnz;
   cudaError_t e = cudaFuncSetAttribute(k_mlp_warm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, nsm = 0, occ = 0;
@@ -593,7 +597,10 @@ cudaError_t launch_mlp_warm(const DevPattern& p, int nsys, const double* A, cons
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mlp_warm, WARM_THREADS, smem);
   if (e != cudaSuccess) return e;
-  const int grid = nsys < nsm * (occ > 0 ? occ : 1) ? nsys : nsm * (occ > 0 ? occ : 1);
+  // every resident CTA holds kTmemCols of the SM's 512 TMEM columns: at most 512 / kTmemCols CTAs per SM,
+  // so that no allocation ever waits for another CTA's
+  occ = occ < 1 ? 1 : (occ > 512 / (int)kTmemCols ? 512 / (int)kTmemCols : occ);
+  const int grid = nsys < nsm * occ ? nsys : nsm * occ;
   k_mlp_warm<<<grid, WARM_THREADS, smem, st>>>(p, nsys, A, rown, coln, corr, (const __nv_bfloat16*)pbf, threshold,
                                                lu0, res, used);
   return cudaGetLastError();

@@ -2,10 +2,14 @@
 // that the benchmark quotes for the solver kernels (FP64 issue, not HBM,
 // bounds them on GB300).  No reference counterpart.
 //
-// Every thread runs kChains independent DFMA chains, so the 64-cycle latency
-// of a dependent DFMA is covered by the chains of one thread and the 8
-// resident CTAs of 256 threads per SM; the rate is the number of lane FMAs
-// over the CUDA-event time of the launch, the best of several launches.
+// Every thread runs CH independent DFMA chains (the loop unrolled 4 times), so
+// the 64-cycle latency of a dependent DFMA is covered many times over by the
+// chains of the SM's resident threads; the rate is the number of lane FMAs
+// over the CUDA-event time of the launch.  Three launch shapes (4, 8 and 16
+// chains per thread at full occupancy) each run 5 times after 2 warm-up
+// launches, and the best rate is kept.  Thread 0 of CTA 0 also reads the SM
+// cycle counter and the global nanosecond timer at its start and end, which
+// gives the SM clock during the launch.
 #include <cuda_runtime.h>
 
 #include <string>
@@ -16,27 +20,69 @@
 namespace bilu {
 namespace {
 
-constexpr int kChains = 8;
 constexpr int kThreads = 256;
 
-__global__ void __launch_bounds__(kThreads) k_dfma_rate(double* __restrict__ sink, int iters, double s) {
-  double a[kChains];
+template <int CH>
+__global__ void __launch_bounds__(kThreads) k_dfma_rate(long long* __restrict__ clk, int iters, double s) {
+  long long c0 = 0, t0 = 0;
+  const bool probe = blockIdx.x == 0 && threadIdx.x == 0;
+  if (probe) {
+    c0 = clock64();
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  }
+  double a[CH];
 #pragma unroll
-  for (int k = 0; k < kChains; ++k) a[k] = 1e-3 * threadIdx.x + k;
-  for (int i = 0; i < iters; ++i) {
+  for (int k = 0; k < CH; ++k) a[k] = 1e-3 * threadIdx.x + k;
+  for (int i = 0; i < iters; i += 4) {
 #pragma unroll
-    for (int k = 0; k < kChains; ++k) a[k] = fma(a[k], s, 1e-9);
+    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+      for (int k = 0; k < CH; ++k) a[k] = fma(a[k], s, 1e-9);
+    }
   }
   double r = 0.0;
 #pragma unroll
-  for (int k = 0; k < kChains; ++k) r += a[k];
-  if (r == -1.0 && sink) sink[0] = r;  // never true (every a[k] stays >= 0): keeps every chain live
+  for (int k = 0; k < CH; ++k) r += a[k];
+  if (probe) {
+    long long t1;
+    const long long c1 = clock64();
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+    clk[0] = c1 - c0;
+    clk[1] = t1 - t0;
+    clk[2] = r == -1.0 ? 1 : 0;  // never true (every a[k] stays >= 0): keeps every chain live
+  }
+}
+
+template <int CH>
+cudaError_t best_rate(cudaStream_t st, int sms, long long* d_clk, cudaEvent_t* ev, double* gflops, double* mhz) {
+  int occ = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_dfma_rate<CH>, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  const int grid = sms * (occ > 0 ? occ : 1), iters = 32768 / CH;
+  for (int rep = 0; rep < 7 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(ev[0], st);
+    k_dfma_rate<CH><<<grid, kThreads, 0, st>>>(d_clk, iters, 0.9999999);
+    e = cudaGetLastError();
+    cudaEventRecord(ev[1], st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+    float ms = 0.0f;
+    long long h[3] = {0, 0, 0};
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    if (e == cudaSuccess) e = cudaMemcpy(h, d_clk, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess || rep < 2 || ms <= 0.0f) continue;  // the first two launches warm up
+    const double g = 2.0 * (double)grid * kThreads * iters * CH / (ms * 1e-3) / 1e9;  // two FLOPs per FMA
+    if (g > *gflops) {
+      *gflops = g;
+      *mhz = h[1] > 0 ? 1e3 * (double)h[0] / (double)h[1] : 0.0;
+    }
+  }
+  return e;
 }
 
 }  // namespace
 }  // namespace bilu
 
-extern "C" bilu_status bilu_probe_fp64_rate(double* h_gflops, void* stream) {
+extern "C" bilu_status bilu_probe_fp64_rate(double* h_gflops, double* h_sm_mhz, void* stream) {
   using namespace bilu;
   if (!h_gflops) return set_error(BILU_ERR_INVALID, "bilu_probe_fp64_rate: NULL output");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -44,25 +90,21 @@ extern "C" bilu_status bilu_probe_fp64_rate(double* h_gflops, void* stream) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return set_error(BILU_ERR_CUDA, std::string("bilu_probe_fp64_rate: ") + cudaGetErrorString(e));
-  const int grid = sms * 8, iters = 4096;
-  cudaEvent_t ev[2];
-  if (cudaEventCreate(&ev[0]) != cudaSuccess || cudaEventCreate(&ev[1]) != cudaSuccess)
-    return set_error(BILU_ERR_CUDA, "bilu_probe_fp64_rate: cudaEventCreate");
-  float best = -1.0f;
-  for (int rep = 0; rep < 7 && e == cudaSuccess; ++rep) {
-    cudaEventRecord(ev[0], st);
-    k_dfma_rate<<<grid, kThreads, 0, st>>>(nullptr, iters, 0.9999999);
-    e = cudaGetLastError();
-    cudaEventRecord(ev[1], st);
-    if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
-    float ms = 0.0f;
-    if (e == cudaSuccess) cudaEventElapsedTime(&ms, ev[0], ev[1]);
-    if (rep >= 2 && (best < 0.0f || ms < best)) best = ms;  // the first two launches warm up
-  }
-  cudaEventDestroy(ev[0]);
-  cudaEventDestroy(ev[1]);
+  long long* d_clk = nullptr;
+  if (cudaMalloc(&d_clk, 4 * sizeof(long long)) != cudaSuccess)
+    return set_error(BILU_ERR_ALLOC, "bilu_probe_fp64_rate: cudaMalloc");
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  e = cudaEventCreate(&ev[0]);
+  if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+  double gflops = 0.0, mhz = 0.0;
+  if (e == cudaSuccess) e = best_rate<4>(st, sms, d_clk, ev, &gflops, &mhz);
+  if (e == cudaSuccess) e = best_rate<8>(st, sms, d_clk, ev, &gflops, &mhz);
+  if (e == cudaSuccess) e = best_rate<16>(st, sms, d_clk, ev, &gflops, &mhz);
+  for (cudaEvent_t x : ev)
+    if (x) cudaEventDestroy(x);
+  cudaFree(d_clk);
   if (e != cudaSuccess) return set_error(BILU_ERR_CUDA, std::string("bilu_probe_fp64_rate: ") + cudaGetErrorString(e));
-  const double fmas = (double)grid * kThreads * iters * kChains;
-  *h_gflops = 2.0 * fmas / (best * 1e-3) / 1e9;  // two FLOPs per FMA
+  *h_gflops = gflops;
+  if (h_sm_mhz) *h_sm_mhz = mhz;
   return BILU_OK;
 }

@@ -55,19 +55,22 @@ def test_gradient_matches_oracle(cuda):
 
 
 def test_tensor_core_inference_matches_oracle(cuda):
-    """The warm start's predictions (64x64 layer on mma.sync, hardware tanh) against the oracle's FP64
-    forward pass on the same BF16 weights."""
+    """The warm start's predictions (64x64 layer on tcgen05.mma with TMEM accumulators, hardware tanh)
+    against the oracle's FP64 forward pass on the same BF16 weights; no system fell back for lack of a
+    completed tensor-core round (ILU residual -1)."""
     import torch
     rp, ci, v, b, plan, V, LU = _setup(cuda, 12)
     with bilu.Mlp(seed=21) as m:
         m.train(plan, V, LU, 50, 2048, 3e-3, seed=2)
         LU0 = torch.empty_like(V)
-        m.warm_start(plan, V, LU0, 1e30)  # accept everything
+        res = torch.empty(V.shape[0], dtype=torch.float64, device=cuda)
+        m.warm_start(plan, V, LU0, 1e30, res)  # accept everything
         LU1 = torch.full_like(V, float("nan"))
         m.warm_start(plan, V, LU1, 1e30)  # a second call gives the same bits
         torch.cuda.synchronize()
         params = m.params()
     got = LU0.cpu().numpy()
+    assert np.all(res.cpu().numpy() >= 0.0)
     H.assert_bitwise(LU1.cpu().numpy(), got, "repeated warm start")
     d = O.find_diag(rp, ci)
     n = len(rp) - 1
