@@ -1,11 +1,13 @@
 // Learned ParILU(0) warm start: a per-nonzero MLP (9 -> 64 -> 64 -> 1, GELU in
 // its tanh form, BF16 weights, FP32 accumulation) that predicts the converged
 // ParILU factors, trained on the GPU by these kernels.  No counterpart in the
-// reference.  Training runs on CUDA cores with an accurate tanh; inference
-// (k_mlp_warm) runs the 64x64 layer on the Blackwell tensor cores (tcgen05.mma
+// reference.  The 64-wide GEMMs run on the Blackwell tensor cores (tcgen05.mma
 // with BF16 operands in shared memory and FP32 accumulators in tensor memory,
-// activations split into BF16 high + low parts so the products keep
-// FP32-level precision) and the hardware tanh approximation.
+// k_tc.cuh; activations and gradients split into BF16 high + low parts so the
+// products keep FP32-level precision): in training (k_mlp_train) the forward
+// 64x64 layer, the backward dh1 = dpre2 W2 and the weight gradient
+// dW2 = dpre2^T H1, with the accurate tanh on the CUDA cores; in inference
+// (k_mlp_warm) the 64x64 layer, with the hardware tanh approximation.
 //
 // Features of nonzero (i, j) of system s, all scaled by d = |a_ii|:
 //   a_ij, a_ii, a_jj, ||A(i,:)||_2, ||A(:,j)||_2 (column over the structurally
@@ -33,6 +35,8 @@ constexpr int OW1 = 0, OB1 = H * NF, OW2 = OB1 + H, OB2 = OW2 + H * H, OW3 = OB2
 static_assert(OB3 + 1 == kMlpParams, "parameter layout");
 
 constexpr unsigned kFull = 0xffffffffu;
+// polls of an mbarrier before a tensor-core round counts as failed (it completes in microseconds)
+constexpr uint32_t kWaitLimit = 1u << 24;
 
 // GELU, tanh form: 0.5 x (1 + tanh(k (x + c x^3))), k = sqrt(2/pi), c = 0.044715
 constexpr float kGk = 0.7978845608028654f, kGc = 0.044715f;
@@ -166,32 +170,123 @@ uint64_t __host__ __device__ __forceinline__ mix64(uint64_t z) {
 constexpr int TB = 128;  // samples (threads) per training block
 constexpr int LD = H + 1;
 
-// One forward + backward pass over a block of samples; weight gradients are
-// reduced over the block and added to `grad` (FP32 atomics), the summed
-// squared error to `loss`.  Samples: explicit global entry indices (s*nnz+e)
-// or, when idx == NULL, hashed from (seed, sample number).
+// BF16 high part of x and the BF16 of what is left (x = hi + lo to about 16 bits)
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(x);
+  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+
+// Sum over the 32 lanes of a warp of 32 values per lane, scattered: lane l
+// returns the warp's sum of v[l] (recursive halving, 31 shuffles).
+__device__ __forceinline__ float warp_reduce_scatter32(const float (&v)[32]) {
+  const int lane = threadIdx.x & 31;
+  float a[16];
+  {
+    const bool up = lane & 16;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const float mine = up ? v[i + 16] : v[i], send = up ? v[i] : v[i + 16];
+      a[i] = mine + __shfl_xor_sync(kFull, send, 16);
+    }
+  }
+#pragma unroll
+  for (int w = 8; w >= 1; w >>= 1) {
+    const bool up = lane & w;
+#pragma unroll
+    for (int i = 0; i < w; ++i) {
+      const float mine = up ? a[i + w] : a[i], send = up ? a[i] : a[i + w];
+      a[i] = mine + __shfl_xor_sync(kFull, send, w);
+    }
+  }
+  return a[0];
+}
+
+// Training block layout (dynamic shared memory, 1024-byte aligned):
+//   A1   [128][64] BF16 hi, lo    K-major: H1 (layer-1 activations), later dpre2
+//   BT   [64][128] BF16 hi, lo    K-major: H1^T (B operand of dW2, K = samples)
+//   AT   [128][128] BF16          K-major: dpre2^T, rows 0..63 high parts, 64..127 low parts
+//   BW   [64][64] BF16            K-major: W2 (row u = output unit)
+//   BWT  [64][64] BF16            K-major: W2^T (row v = input unit)
+//   W1   [64][12] FP32            W1[v][0..8], b1[v], 0, 0
+//   BWV  [64] float2              (b2[u], w3[u])
+//   X    [128][9] FP32            features
+//   G1   [128][65] FP32           gelu'(pre1), later dpre1
+//   RED  [3][4][64] FP32          per-warp sums of db2, dW3, db1
+constexpr int TR_A1 = 0, TR_BT = TR_A1 + 2 * TB * H * 2, TR_AT = TR_BT + 2 * H * TB * 2, TR_BW = TR_AT + TB * TB * 2;
+constexpr int TR_BWT = TR_BW + H * H * 2, TR_W1 = TR_BWT + H * H * 2, TR_BWV = TR_W1 + H * 12 * 4;
+constexpr int TR_X = TR_BWV + H * 8, TR_G1 = TR_X + TB * NF * 4, TR_RED = TR_G1 + TB * LD * 4;
+constexpr int TR_SMEM = TR_RED + 3 * 4 * H * 4;
+constexpr uint32_t kTrainTmemCols = 256;  // D1 pre2 | D2 dh1 | D3, D4 the two halves of dW2
+static_assert(TR_W1 % 16 == 0 && TR_X % 16 == 0, "aligned blocks");
+
+// One forward + backward pass over a block of 128 samples (thread = sample) with
+// the three 64-wide GEMMs on the tensor cores (tcgen05.mma, BF16 operands
+// split into high and low parts, FP32 accumulators in TMEM):
+//   forward   pre2 = H1 W2^T                 (M = 128 samples, N = 64, K = 64)
+//   backward  dh1  = dpre2 W2                (M = 128 samples, N = 64, K = 64)
+//             dW2  = dpre2^T H1              (M = 128: the 64 units' high and low
+//                                             parts stacked, N = 64, K = 128 samples)
+// Layer 1, the activations and the output layer run on the CUDA cores in FP32
+// with the accurate tanh.  Per-unit sums over the block (db1, db2, dW3) are
+// reduce-scattered across each warp; dW1 is reduced over the block in shared
+// memory; everything is added to `grad` (FP32 atomics), the summed squared
+// error to `loss`.  Samples: explicit global entry indices (s*nnz+e) or, when
+// idx == NULL, hashed from (seed, sample number).  A tensor-core round that
+// does not complete within the bounded wait adds NaN to `loss` and ends the
+// block.
 __global__ void __launch_bounds__(TB) k_mlp_train(const DevPattern P, int nsys, const double* __restrict__ A,
                                                   const double* __restrict__ LUt, const float* __restrict__ rown,
                                                   const float* __restrict__ coln, const float* __restrict__ corr,
                                                   const __nv_bfloat16* __restrict__ pbf, int nsample,
                                                   const int* __restrict__ idx, uint64_t seed, float scale,
                                                   float* __restrict__ grad, float* __restrict__ loss) {
-  extern __shared__ __align__(16) float sm[];
-  float* sp = sm;                          // kMlpParams (padded to 4)
-  float* X = sp + ((kMlpParams + 3) & ~3);  // TB * NF
-  float* H1 = X + TB * NF;                 // TB * LD
-  float* G1 = H1 + TB * LD;                // TB * LD (gelu', then dpre1)
-  float* P2 = G1 + TB * LD;                // TB * LD (pre2, then d*h2)
-  float* D2 = P2 + TB * LD;                // TB * LD (dpre2)
-  float* DO = D2 + TB * LD;                // TB
-  __shared__ float s_loss[TB / 32];
-  stage_params(pbf, sp);
+  extern __shared__ __align__(1024) unsigned char smt[];
+  __shared__ uint64_t s_mbar;
+  __shared__ uint32_t s_tmem;
+  __shared__ float s_loss[TB / 32], s_do[TB / 32];
+  __shared__ int s_fail;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  float* X = reinterpret_cast<float*>(smt + TR_X);
+  float* G1 = reinterpret_cast<float*>(smt + TR_G1);
+  float* RED = reinterpret_cast<float*>(smt + TR_RED);
+  // ---- weights
+  {
+    const uint4* w2g = reinterpret_cast<const uint4*>(pbf + OW2);
+    for (int k = t; k < H * 8; k += TB) {
+      const int u = k >> 3, c = k & 7;
+      *reinterpret_cast<uint4*>(smt + TR_BW + tc::kmajor_off(u, 8 * c, H)) = w2g[k];
+    }
+    for (int k = t; k < H * H; k += TB) {  // W2^T: element (v, u) = W2[u][v]
+      const int u = k >> 6, v = k & 63;
+      *reinterpret_cast<__nv_bfloat16*>(smt + TR_BWT + tc::kmajor_off(v, u, H)) = pbf[OW2 + k];
+    }
+    float* w1 = reinterpret_cast<float*>(smt + TR_W1);
+    for (int k = t; k < H * 12; k += TB) {
+      const int v = k / 12, c = k % 12;
+      w1[k] = c < NF ? __bfloat162float(pbf[OW1 + v * NF + c]) : (c == NF ? __bfloat162float(pbf[OB1 + v]) : 0.0f);
+    }
+    float2* bwv = reinterpret_cast<float2*>(smt + TR_BWV);
+    for (int u = t; u < H; u += TB) bwv[u] = make_float2(__bfloat162float(pbf[OB2 + u]), __bfloat162float(pbf[OW3 + u]));
+  }
+  if (t == 0) {
+    tc::mbar_init(&s_mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_fail = 0;
+  }
+  if (warp == 0) tc::alloc(&s_tmem, kTrainTmemCols);
+  tc::fence_before_sync();
   __syncthreads();
-  const int t = threadIdx.x;
+  tc::fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+  const float4* w1v = reinterpret_cast<const float4*>(smt + TR_W1);
+  const float2* bwv = reinterpret_cast<const float2*>(smt + TR_BWV);
+  const float b3 = __bfloat162float(pbf[OB3]);
+  // ---- sample, features, target
   const long long q = (long long)blockIdx.x * TB + t;
   const bool live = q < nsample;
-  float err2 = 0.0f;
-  float* xr = X + t * NF;
+  float f[NF];
+  float ytrue = 0.0f;
   if (live) {
     long long g;
     if (idx) {
@@ -203,83 +298,227 @@ __global__ void __launch_bounds__(TB) k_mlp_train(const DevPattern P, int nsys, 
     const int s = (int)(g / P.nnz), e = (int)(g % P.nnz);
     const Feat ft = features(P, s, e, A, rown, coln, corr);
 #pragma unroll
-    for (int k = 0; k < NF; ++k) xr[k] = ft.f[k];
+    for (int k = 0; k < NF; ++k) f[k] = ft.f[k];
     const double denom = ft.a * (double)ft.base;
-    const float ytrue = denom != 0.0 ? (float)(LUt[g] / denom - 1.0) : 0.0f;
-    const float out = mlp_forward(sp, xr, H1 + t * LD, G1 + t * LD, P2 + t * LD);
-    const float diff = out - ytrue;
-    err2 = diff * diff;
-    const float dout = 2.0f * diff * scale;
-    DO[t] = dout;
-    // layer 3 and 2
-    float* p2 = P2 + t * LD;
-    float* d2 = D2 + t * LD;
-    for (int u = 0; u < H; ++u) {
-      const float pre = p2[u];
-      d2[u] = dout * sp[OW3 + u] * gelu_d(pre);
-      p2[u] = dout * gelu(pre);  // contribution to dW3
-    }
-    // dh1 = W2^T dpre2, dpre1 = dh1 * gelu'(pre1)
-    float dp[H];
-#pragma unroll
-    for (int u = 0; u < H; ++u) dp[u] = d2[u];
-    float* g1 = G1 + t * LD;
-    for (int v = 0; v < H; ++v) {
-      float acc = 0.0f;
-#pragma unroll
-      for (int u = 0; u < H; ++u) acc = fmaf(sp[OW2 + u * H + v], dp[u], acc);
-      g1[v] = acc * g1[v];
-    }
+    ytrue = denom != 0.0 ? (float)(LUt[g] / denom - 1.0) : 0.0f;
   } else {
-    DO[t] = 0.0f;
-    for (int k = 0; k < NF; ++k) xr[k] = 0.0f;
-    for (int u = 0; u < H; ++u) {
-      H1[t * LD + u] = 0.0f;
-      G1[t * LD + u] = 0.0f;
-      P2[t * LD + u] = 0.0f;
-      D2[t * LD + u] = 0.0f;
-    }
-  }
-  // loss
-  float l = err2;
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) l += __shfl_down_sync(kFull, l, off);
-  if ((t & 31) == 0) s_loss[t >> 5] = l;
+    for (int k = 0; k < NF; ++k) f[k] = 0.0f;
+  }
+#pragma unroll
+  for (int k = 0; k < NF; ++k) X[t * NF + k] = live ? f[k] : 0.0f;
+  // ---- layer 1 (CUDA cores): H1 hi / lo into A1 (row t) and BT (column t), gelu'(pre1) into G1
+  __nv_bfloat16* bth = reinterpret_cast<__nv_bfloat16*>(smt + TR_BT);
+  __nv_bfloat16* btl = reinterpret_cast<__nv_bfloat16*>(smt + TR_BT + H * TB * 2);
+#pragma unroll 1
+  for (int c = 0; c < H / 8; ++c) {
+    __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+    for (int d = 0; d < 8; ++d) {
+      const int v = 8 * c + d;
+      const float4 wa = w1v[v * 3], wb = w1v[v * 3 + 1], wc = w1v[v * 3 + 2];
+      const float w[NF] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w, wc.x};
+      float pre = wc.y;
+#pragma unroll
+      for (int k = 0; k < NF; ++k) pre = fmaf(w[k], f[k], pre);
+      const float h = live ? gelu(pre) : 0.0f;
+      G1[t * LD + v] = live ? gelu_d(pre) : 0.0f;
+      split_bf16(h, hi[d], lo[d]);
+      const uint32_t bo = tc::kmajor_off(v, t, TB) / 2;
+      bth[bo] = hi[d];
+      btl[bo] = lo[d];
+    }
+    const uint32_t off = tc::kmajor_off(t, 8 * c, H);
+    *reinterpret_cast<uint4*>(smt + TR_A1 + off) = *reinterpret_cast<const uint4*>(hi);
+    *reinterpret_cast<uint4*>(smt + TR_A1 + TB * H * 2 + off) = *reinterpret_cast<const uint4*>(lo);
+  }
+  const uint32_t a1h = tc::smem_u32(smt + TR_A1), a1l = a1h + TB * H * 2;
+  const uint32_t bth_a = tc::smem_u32(smt + TR_BT), btl_a = bth_a + H * TB * 2;
+  const uint32_t at_a = tc::smem_u32(smt + TR_AT), bw_a = tc::smem_u32(smt + TR_BW), bwt_a = tc::smem_u32(smt + TR_BWT);
+  constexpr uint32_t kSbo64 = H * 16, kSbo128 = TB * 16;
+  const uint32_t id128 = tc::idesc_bf16(128, H);
+  // ---- forward layer 2 on the tensor cores: D1 = H1 W2^T
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
   __syncthreads();
   if (t == 0) {
-    float sum = 0.0f;
-    for (int w = 0; w < TB / 32; ++w) sum += s_loss[w];
-    atomicAdd(loss, sum * scale);
+    tc::fence_after_sync();
+#pragma unroll
+    for (int j = 0; j < H / 16; ++j)
+      tc::mma_bf16(tmem, tc::sdesc(a1h + 256 * j, kSbo64), tc::sdesc(bw_a + 256 * j, kSbo64), id128, j > 0);
+#pragma unroll
+    for (int j = 0; j < H / 16; ++j)
+      tc::mma_bf16(tmem, tc::sdesc(a1l + 256 * j, kSbo64), tc::sdesc(bw_a + 256 * j, kSbo64), id128, 1);
+    tc::commit(&s_mbar);
   }
-  // block-reduced weight gradients
-  for (int k = t; k < H * H; k += TB) {  // dW2[u][v] = sum_t dpre2[t][u] * h1[t][v]
-    const int u = k / H, v = k % H;
-    float acc = 0.0f;
-    for (int r = 0; r < TB; ++r) acc = fmaf(D2[r * LD + u], H1[r * LD + v], acc);
-    atomicAdd(grad + OW2 + k, acc);
-  }
-  for (int k = t; k < H * NF; k += TB) {  // dW1[u][f] = sum_t dpre1[t][u] * x[t][f]
-    const int u = k / NF, f = k % NF;
-    float acc = 0.0f;
-    for (int r = 0; r < TB; ++r) acc = fmaf(G1[r * LD + u], X[r * NF + f], acc);
-    atomicAdd(grad + OW1 + k, acc);
-  }
-  if (t < H) {
-    float a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
-    for (int r = 0; r < TB; ++r) {
-      a1 += G1[r * LD + t];
-      a2 += D2[r * LD + t];
-      a3 += P2[r * LD + t];
+  if (!tc::mbar_wait(&s_mbar, 0, kWaitLimit)) s_fail = 1;  // 1 + the parity of the phase that did not complete
+  tc::fence_after_sync();
+  __syncthreads();
+  if (s_fail) {
+    if (t == 0) atomicAdd(loss, __int_as_float(0x7fc00000));
+  } else {
+    // ---- output layer, loss, dout
+    float out = b3;
+#pragma unroll 1
+    for (int c = 0; c < H / 16; ++c) {
+      float acc[16];
+      tc::ld16(trow + 16 * c, acc);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const float2 bw = bwv[16 * c + k];
+        out = fmaf(bw.y, gelu(acc[k] + bw.x), out);
+      }
     }
-    atomicAdd(grad + OB1 + t, a1);
-    atomicAdd(grad + OB2 + t, a2);
-    atomicAdd(grad + OW3 + t, a3);
+    const float diff = out - ytrue;
+    const float err2 = live ? diff * diff : 0.0f;
+    const float dout = live ? 2.0f * diff * scale : 0.0f;
+    // ---- dpre2 = dout w3 gelu'(pre2) into A1 (row t) and AT (column t); per-unit sums of dpre2 (db2)
+    // and of dout gelu(pre2) (dW3), reduce-scattered over the warp: lane l holds units l and 32 + l
+    __nv_bfloat16* ath = reinterpret_cast<__nv_bfloat16*>(smt + TR_AT);
+    float rs_db2[2], rs_dw3[2];
+#pragma unroll 1
+    for (int c2 = 0; c2 < 2; ++c2) {
+      float dp[32], dw[32];
+#pragma unroll
+      for (int h16 = 0; h16 < 2; ++h16) {
+        float acc[16];
+        tc::ld16(trow + 32 * c2 + 16 * h16, acc);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const int u = 32 * c2 + 16 * h16 + k;
+          const float pre = acc[k] + bwv[u].x;
+          dp[16 * h16 + k] = dout * bwv[u].y * gelu_d(pre);
+          dw[16 * h16 + k] = dout * gelu(pre);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+          const int u = 32 * c2 + 8 * c + d;
+          split_bf16(dp[8 * c + d], hi[d], lo[d]);
+          ath[tc::kmajor_off(u, t, TB) / 2] = hi[d];
+          ath[tc::kmajor_off(H + u, t, TB) / 2] = lo[d];
+        }
+        const uint32_t off = tc::kmajor_off(t, 32 * c2 + 8 * c, H);
+        *reinterpret_cast<uint4*>(smt + TR_A1 + off) = *reinterpret_cast<const uint4*>(hi);
+        *reinterpret_cast<uint4*>(smt + TR_A1 + TB * H * 2 + off) = *reinterpret_cast<const uint4*>(lo);
+      }
+      rs_db2[c2] = warp_reduce_scatter32(dp);
+      rs_dw3[c2] = warp_reduce_scatter32(dw);
+    }
+    // ---- backward GEMMs on the tensor cores: D2 = dpre2 W2, D3 / D4 = dpre2^T (hi | lo stacked) H1 (hi / lo)
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (t == 0) {
+      tc::fence_after_sync();
+#pragma unroll
+      for (int j = 0; j < H / 16; ++j)
+        tc::mma_bf16(tmem + 64, tc::sdesc(a1h + 256 * j, kSbo64), tc::sdesc(bwt_a + 256 * j, kSbo64), id128, j > 0);
+#pragma unroll
+      for (int j = 0; j < H / 16; ++j)
+        tc::mma_bf16(tmem + 64, tc::sdesc(a1l + 256 * j, kSbo64), tc::sdesc(bwt_a + 256 * j, kSbo64), id128, 1);
+#pragma unroll
+      for (int j = 0; j < TB / 16; ++j)
+        tc::mma_bf16(tmem + 128, tc::sdesc(at_a + 256 * j, kSbo128), tc::sdesc(bth_a + 256 * j, kSbo128), id128,
+                     j > 0);
+#pragma unroll
+      for (int j = 0; j < TB / 16; ++j)
+        tc::mma_bf16(tmem + 192, tc::sdesc(at_a + 256 * j, kSbo128), tc::sdesc(btl_a + 256 * j, kSbo128), id128,
+                     j > 0);
+      tc::commit(&s_mbar);
+    }
+    // loss and the sum of dout (db3) while the tensor cores run
+    float l = err2, dsum = dout;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      l += __shfl_down_sync(kFull, l, off);
+      dsum += __shfl_down_sync(kFull, dsum, off);
+    }
+    if (lane == 0) {
+      s_loss[warp] = l;
+      s_do[warp] = dsum;
+    }
+    RED[(0 * 4 + warp) * H + lane] = rs_db2[0];
+    RED[(0 * 4 + warp) * H + 32 + lane] = rs_db2[1];
+    RED[(1 * 4 + warp) * H + lane] = rs_dw3[0];
+    RED[(1 * 4 + warp) * H + 32 + lane] = rs_dw3[1];
+    if (!tc::mbar_wait(&s_mbar, 1, kWaitLimit)) s_fail = 2;
+    tc::fence_after_sync();
+    __syncthreads();
+    if (s_fail) {
+      if (t == 0) atomicAdd(loss, __int_as_float(0x7fc00000));
+    } else {
+      // ---- dpre1 = dh1 * gelu'(pre1) into G1; per-unit sums of dpre1 (db1)
+      float rs_db1[2];
+#pragma unroll 1
+      for (int c2 = 0; c2 < 2; ++c2) {
+        float dp[32];
+#pragma unroll
+        for (int h16 = 0; h16 < 2; ++h16) {
+          float acc[16];
+          tc::ld16(trow + 64 + 32 * c2 + 16 * h16, acc);
+#pragma unroll
+          for (int k = 0; k < 16; ++k) {
+            const int v = 32 * c2 + 16 * h16 + k;
+            const float d = acc[k] * G1[t * LD + v];
+            G1[t * LD + v] = d;
+            dp[16 * h16 + k] = d;
+          }
+        }
+        rs_db1[c2] = warp_reduce_scatter32(dp);
+      }
+      RED[(2 * 4 + warp) * H + lane] = rs_db1[0];
+      RED[(2 * 4 + warp) * H + 32 + lane] = rs_db1[1];
+      // ---- dW2: row r of D3 + D4 is unit r % 64's share (high part for r < 64, low part above)
+      {
+        const int u = (32 * warp + lane) & 63;
+#pragma unroll 1
+        for (int c = 0; c < H / 16; ++c) {
+          float d3[16], d4[16];
+          tc::ld16(trow + 128 + 16 * c, d3);
+          tc::ld16(trow + 192 + 16 * c, d4);
+#pragma unroll
+          for (int k = 0; k < 16; ++k) atomicAdd(grad + OW2 + u * H + 16 * c + k, d3[k] + d4[k]);
+        }
+      }
+      __syncthreads();
+      if (t == 0) {
+        float a = 0.0f, d = 0.0f;
+        for (int w = 0; w < TB / 32; ++w) {
+          a += s_loss[w];
+          d += s_do[w];
+        }
+        atomicAdd(loss, a * scale);
+        atomicAdd(grad + OB3, d);
+      }
+      if (t < H) {
+        float db2 = 0.0f, dw3 = 0.0f, db1 = 0.0f;
+        for (int w = 0; w < TB / 32; ++w) {
+          db2 += RED[(0 * 4 + w) * H + t];
+          dw3 += RED[(1 * 4 + w) * H + t];
+          db1 += RED[(2 * 4 + w) * H + t];
+        }
+        atomicAdd(grad + OB2 + t, db2);
+        atomicAdd(grad + OW3 + t, dw3);
+        atomicAdd(grad + OB1 + t, db1);
+      }
+      for (int k = t; k < H * NF; k += TB) {  // dW1[u][f] = sum_t dpre1[t][u] * x[t][f]
+        const int u = k / NF, fi = k % NF;
+        float acc = 0.0f;
+        for (int r = 0; r < TB; ++r) acc = fmaf(G1[r * LD + u], X[r * NF + fi], acc);
+        atomicAdd(grad + OW1 + k, acc);
+      }
+    }
   }
-  if (t == H) {
-    float a = 0.0f;
-    for (int r = 0; r < TB; ++r) a += DO[r];
-    atomicAdd(grad + OB3, a);
-  }
+  // a round that timed out may still be in flight: wait once more (bounded) before freeing its columns
+  if (s_fail) tc::mbar_wait(&s_mbar, (uint32_t)(s_fail - 1), kWaitLimit);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::dealloc(tmem, kTrainTmemCols);
 }
 
 // Adam on the FP32 master parameters; refreshes the BF16 copy.
@@ -346,7 +585,6 @@ constexpr int WARM_THREADS = 128;
 constexpr int WT_AH = 0, WT_AL = WT_AH + 128 * H * 2, WT_B = WT_AL + 128 * H * 2, WT_W1 = WT_B + H * H * 2;
 constexpr int WT_BW = WT_W1 + H * 12 * 4, WT_LU = WT_BW + H * 8;
 constexpr uint32_t kTmemCols = 64;
-constexpr uint32_t kWaitLimit = 1u << 24;
 static_assert(WT_W1 % 16 == 0 && WT_LU % 16 == 0, "aligned operand blocks");
 
 __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, int nsys,
@@ -545,9 +783,7 @@ cudaError_t launch_mlp_rowstats(const DevPattern& p, int nsys, const double* A, 
   return cudaGetLastError();
 }
 
-size_t mlp_train_smem() {
-  return sizeof(float) * (((kMlpParams + 3) & ~3) + TB * NF + 4 * TB * LD + TB);
-}
+size_t mlp_train_smem() { return TR_SMEM; }
 
 cudaError_t launch_mlp_train(const DevPattern& p, int nsys, const double* A, const double* LUt, const float* rown,
                              const float* coln, const float* corr, const void* pbf, int nsample, const int* idx,
