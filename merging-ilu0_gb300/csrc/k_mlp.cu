@@ -21,6 +21,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "bilu_internal.h"
@@ -565,27 +566,50 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
 }
 
 // Warm start: persistent CTAs of 128 threads over the systems (the network's
-// weights are staged once per CTA).  Entries with no dependency pairs on or
-// above the diagonal converge to a_ij exactly and are copied.  The others go
-// through the network in tiles of 128, one entry per thread:
+// weights are staged once per CTA).  Every system's LU0 starts as a copy of A
+// (exact for the entries on or above the diagonal without dependency pairs,
+// which converge to a_ij).  The other entries go through the network in tiles
+// of 128, one entry per thread:
 //   layer 1 (9 -> 64) on the CUDA cores, GELU, the activations split into BF16
 //   high and low parts (h = hi + lo to about 16 bits) and stored as the two
 //   128 x 64 A operands of the tensor core (K-major, k_tc.cuh layout);
 //   layer 2 (64 x 64) as 8 tcgen05.mma of M = 128, N = 64, K = 16 (hi and lo
 //   against W2 in BF16, FP32 accumulation in 64 TMEM columns), issued by one
-//   thread and completed through an mbarrier;
+//   thread and completed through an mbarrier; while it runs, every thread
+//   gathers the features of its entry of the next tile;
 //   every thread reads its own row of the accumulator (tcgen05.ld, lane = row),
-//   adds b2, GELU, and the output layer's dot product with w3.
-// The ILU residual ||(A - L0 U0)|_S||_F / ||A||_F then decides between the
-// prediction and the plain initialisation lu0 = A.
+//   adds b2, GELU, and the output layer's dot product with w3, and writes its
+//   prediction into LU0.
+// The ILU residual ||(A - L0 U0)|_S||_F / ||A||_F of the written factors then
+// decides between the prediction and the plain initialisation (the predicted
+// entries are copied back from A).  Shared memory holds only the operands and
+// weights (44 KB), so five CTAs share an SM.
 // The mbarrier waits are bounded: a CTA whose tensor-core work does not
 // complete in time stops using it and writes the plain initialisation
 // (used = 0, ILU residual -1) for its remaining systems.
 constexpr int WARM_THREADS = 128;
 constexpr int WT_AH = 0, WT_AL = WT_AH + 128 * H * 2, WT_B = WT_AL + 128 * H * 2, WT_W1 = WT_B + H * H * 2;
-constexpr int WT_BW = WT_W1 + H * 12 * 4, WT_LU = WT_BW + H * 8;
+constexpr int WT_BW = WT_W1 + H * 12 * 4, WT_SMEM = WT_BW + H * 8;
 constexpr uint32_t kTmemCols = 64;
-static_assert(WT_W1 % 16 == 0 && WT_LU % 16 == 0, "aligned operand blocks");
+static_assert(WT_W1 % 16 == 0, "aligned operand blocks");
+
+// features of predicted entry q of system s (zeros past the last one)
+__device__ __forceinline__ void warm_features(const DevPattern& P, int s, int q, const double* __restrict__ A,
+                                              const float* __restrict__ rown, const float* __restrict__ coln,
+                                              const float* __restrict__ corr, float (&f)[NF], double& ab, int& e) {
+  if (q < P.n_mlp) {
+    e = P.mlp_ent[q];
+    const Feat ft = features(P, s, e, A, rown, coln, corr);
+#pragma unroll
+    for (int k = 0; k < NF; ++k) f[k] = ft.f[k];
+    ab = ft.a * (double)ft.base;
+  } else {
+    e = -1;
+    ab = 0.0;
+#pragma unroll
+    for (int k = 0; k < NF; ++k) f[k] = 0.0f;
+  }
+}
 
 __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, int nsys,
                                                            const double* __restrict__ A,
@@ -630,7 +654,6 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
   const float4* w1v = reinterpret_cast<const float4*>(smraw + WT_W1);
   const float2* bw = reinterpret_cast<const float2*>(smraw + WT_BW);
   const float b3 = __bfloat162float(pbf[OB3]);
-  double* lu = reinterpret_cast<double*>(smraw + WT_LU);
   const uint32_t a_hi = tc::smem_u32(smraw + WT_AH), a_lo = tc::smem_u32(smraw + WT_AL);
   const uint32_t b_w2 = tc::smem_u32(smraw + WT_B);
   constexpr uint32_t kSbo = H * 16;  // K = 64: 8-row groups 1024 bytes apart
@@ -639,27 +662,16 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
   const int ntile = (P.n_mlp + WARM_THREADS - 1) / WARM_THREADS;
   uint32_t phase = 0;
   for (int s = blockIdx.x; s < nsys; s += gridDim.x) {
-    __syncthreads();  // the previous system's lu and s_ok no longer read
     const double* As = A + (size_t)s * P.nnz;
-    for (int e = tid; e < P.nnz; e += WARM_THREADS) lu[e] = As[e];  // exact for the copied entries
+    double* Ls = LU0 + (size_t)s * P.nnz;
+    for (int e = tid; e < P.nnz; e += WARM_THREADS) Ls[e] = As[e];
     const bool failed = s_fail != 0;  // uniform: written before the last barrier
-    __syncthreads();
+    float f[NF];
+    double ab;
+    int e;
+    if (!failed) warm_features(P, s, tid, A, rown, coln, corr, f, ab, e);
+    __syncthreads();  // the copy of A is complete before any prediction overwrites it
     for (int tile = 0; tile < ntile && !failed; ++tile) {
-      const int q = tile * WARM_THREADS + tid;
-      const bool live = q < P.n_mlp;
-      float f[NF];
-      double ab = 0.0;
-      int e = -1;
-      if (live) {
-        e = P.mlp_ent[q];
-        const Feat ft = features(P, s, e, A, rown, coln, corr);
-#pragma unroll
-        for (int k = 0; k < NF; ++k) f[k] = ft.f[k];
-        ab = ft.a * (double)ft.base;
-      } else {
-#pragma unroll
-        for (int k = 0; k < NF; ++k) f[k] = 0.0f;
-      }
       // layer 1 on the CUDA cores, 8 hidden units at a time into one 16-byte chunk of each A operand
 #pragma unroll 1
       for (int c = 0; c < H / 8; ++c) {
@@ -701,6 +713,10 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
           tc::mma_bf16(tmem, tc::sdesc(a_lo + 256 * j, kSbo), tc::sdesc(b_w2 + 256 * j, kSbo), idesc, 1);
         tc::commit(&s_mbar);
       }
+      // the next tile's features while the tensor core runs
+      const double ab_cur = ab;
+      const int e_cur = e;
+      if (tile + 1 < ntile) warm_features(P, s, (tile + 1) * WARM_THREADS + tid, A, rown, coln, corr, f, ab, e);
       const bool done = tc::mbar_wait(&s_mbar, phase, kWaitLimit);
       phase ^= 1u;
       if (!done) s_fail = 1;
@@ -719,25 +735,25 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
           out = fmaf(q2.y, gelu_fast(acc[k] + q2.x), out);
         }
       }
-      if (live) lu[e] = ab * (1.0 + (double)(out + b3));
+      if (e_cur >= 0) Ls[e_cur] = ab_cur * (1.0 + (double)(out + b3));
       tc::fence_before_sync();
     }
-    __syncthreads();
+    __syncthreads();  // every prediction of this system written (block-visible) before the residual reads
     const bool fail = s_fail != 0;
     // residual of the warm start: (A - LU)_ij = a_ij - sum_{k<min(i,j)} l_ik u_kj - (l_ij u_jj | u_ij)
     double num = 0.0, den = 0.0;
     if (!fail) {
-      for (int e = tid; e < P.nnz; e += WARM_THREADS) {
-        const int i = P.row_of[e], j = P.ci[e];
+      for (int e2 = tid; e2 < P.nnz; e2 += WARM_THREADS) {
+        const int i = P.row_of[e2], j = P.ci[e2];
         double acc = 0.0;
-        for (int q = P.dep_ptr[e]; q < P.dep_ptr[e + 1]; ++q) {
+        for (int q = P.dep_ptr[e2]; q < P.dep_ptr[e2 + 1]; ++q) {
           const int2 d = P.dep[q];
-          acc = fma(lu[d.x], lu[d.y], acc);
+          acc = fma(Ls[d.x], Ls[d.y], acc);
         }
-        acc = (j < i) ? fma(lu[e], lu[P.diag[j]], acc) : acc + lu[e];
-        const double rr = As[e] - acc;
+        acc = (j < i) ? fma(Ls[e2], Ls[P.diag[j]], acc) : acc + Ls[e2];
+        const double rr = As[e2] - acc;
         num = fma(rr, rr, num);
-        den = fma(As[e], As[e], den);
+        den = fma(As[e2], As[e2], den);
       }
     }
 #pragma unroll
@@ -762,8 +778,13 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
       if (used) used[s] = s_ok;
     }
     __syncthreads();
-    const int ok = s_ok;
-    for (int e = tid; e < P.nnz; e += WARM_THREADS) LU0[(size_t)s * P.nnz + e] = ok ? lu[e] : As[e];
+    if (!s_ok) {  // fallback: the predicted entries back to A's values
+      for (int q = tid; q < P.n_mlp; q += WARM_THREADS) {
+        const int e2 = P.mlp_ent[q];
+        Ls[e2] = As[e2];
+      }
+    }
+    __syncthreads();  // s_ok and the residual slots are free for the next system
   }
   // a tensor-core round that timed out may still be in flight: wait for it once more (bounded) before the
   // accumulator columns are freed
@@ -825,17 +846,27 @@ cudaError_t launch_mlp_warm(const DevPattern& p, int nsys, const double* A, cons
                             const float* corr, const void* pbf, double threshold, double* lu0, double* res, int* used,
                             cudaStream_t st) {
   if (nsys == 0) return cudaSuccess;
-  const size_t smem = WT_LU + sizeof(double) * p.nnz;
+  const size_t smem = WT_SMEM;
   cudaError_t e = cudaFuncSetAttribute(k_mlp_warm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  int dev = 0, nsm = 0, occ = 0;
+  // CTAs per SM from the kernel's own resources (measured on GB300: the occupancy calculator reports
+  // one CTA per SM for this tcgen05 kernel, where its shared memory admits five); every resident CTA
+  // holds kTmemCols of the SM's 512 TMEM columns, so at most 512 / kTmemCols, and no allocation ever
+  // waits for another CTA's
+  int dev = 0, nsm = 0, per_sm = 0, reserved = 0, thr_sm = 0, regs_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mlp_warm, WARM_THREADS, smem);
+  cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, k_mlp_warm);
   if (e != cudaSuccess) return e;
-  // every resident CTA holds kTmemCols of the SM's 512 TMEM columns: at most 512 / kTmemCols CTAs per SM,
-  // so that no allocation ever waits for another CTA's
-  occ = occ < 1 ? 1 : (occ > 512 / (int)kTmemCols ? 512 / (int)kTmemCols : occ);
+  int occ = per_sm / (int)(smem + fa.sharedSizeBytes + reserved);
+  occ = std::min(occ, thr_sm / WARM_THREADS);
+  occ = std::min(occ, regs_sm / std::max(1, ((fa.numRegs + 7) / 8 * 8) * WARM_THREADS));
+  occ = std::max(1, std::min(occ, 512 / (int)kTmemCols));
   const int grid = nsys < nsm * occ ? nsys : nsm * occ;
   k_mlp_warm<<<grid, WARM_THREADS, smem, st>>>(p, nsys, A, rown, coln, corr, (const __nv_bfloat16*)pbf, threshold,
                                                lu0, res, used);
