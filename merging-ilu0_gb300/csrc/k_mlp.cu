@@ -569,29 +569,33 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
 // weights are staged once per CTA).  Every system's LU0 starts as a copy of A
 // (exact for the entries on or above the diagonal without dependency pairs,
 // which converge to a_ij).  The other entries go through the network in tiles
-// of 128, one entry per thread:
-//   layer 1 (9 -> 64) on the CUDA cores, GELU, the activations split into BF16
-//   high and low parts (h = hi + lo to about 16 bits) and stored as the two
-//   128 x 64 A operands of the tensor core (K-major, k_tc.cuh layout);
-//   layer 2 (64 x 64) as 8 tcgen05.mma of M = 128, N = 64, K = 16 (hi and lo
-//   against W2 in BF16, FP32 accumulation in 64 TMEM columns), issued by one
-//   thread and completed through an mbarrier; while it runs, every thread
-//   gathers the features of its entry of the next tile;
-//   every thread reads its own row of the accumulator (tcgen05.ld, lane = row),
-//   adds b2, GELU, and the output layer's dot product with w3, and writes its
-//   prediction into LU0.
+// of 128, one entry per thread, both hidden layers on the tensor core
+// (tcgen05.mma, M = 128 entries, N = 64, BF16 operands split into high and low
+// parts so that x = hi + lo to about 16 bits, FP32 accumulation in the same 64
+// TMEM columns), issued by one thread and completed through an mbarrier:
+//   layer 1: the features (9, then 1.0 for the bias, zero-padded to K = 16)
+//   against W1 | b1 (BF16): 2 MMAs;
+//   every thread reads its row of pre1 (tcgen05.ld, lane = row), GELU, and
+//   stores the activations as the 128 x 64 A operands of layer 2;
+//   layer 2: hi and lo against W2 (BF16), K = 64: 8 MMAs; while they run,
+//   every thread gathers the features of its entry of the next tile;
+//   every thread reads its row of pre2, adds b2, GELU, the output layer's dot
+//   product with w3, and writes its prediction into LU0.
 // The ILU residual ||(A - L0 U0)|_S||_F / ||A||_F of the written factors then
 // decides between the prediction and the plain initialisation (the predicted
 // entries are copied back from A).  Shared memory holds only the operands and
-// weights (44 KB), so five CTAs share an SM.
+// weights (42.5 KB; the layer-1 operand lives in the layer-2 low-part buffer,
+// which is free until layer 1 has completed), so five CTAs share an SM.
 // The mbarrier waits are bounded: a CTA whose tensor-core work does not
 // complete in time stops using it and writes the plain initialisation
 // (used = 0, ILU residual -1) for its remaining systems.
 constexpr int WARM_THREADS = 128;
-constexpr int WT_AH = 0, WT_AL = WT_AH + 128 * H * 2, WT_B = WT_AL + 128 * H * 2, WT_W1 = WT_B + H * H * 2;
-constexpr int WT_BW = WT_W1 + H * 12 * 4, WT_SMEM = WT_BW + H * 8;
+constexpr int KX = 16;  // layer-1 K: 9 features, the bias input, zero padding
+constexpr int WT_AH = 0, WT_AL = WT_AH + 128 * H * 2, WT_B = WT_AL + 128 * H * 2, WT_B1 = WT_B + H * H * 2;
+constexpr int WT_BW = WT_B1 + H * KX * 2, WT_SMEM = WT_BW + H * 8;
+constexpr int WT_XH = WT_AL, WT_XL = WT_AL + 128 * KX * 2;  // layer-1 operand, aliasing the layer-2 low part
 constexpr uint32_t kTmemCols = 64;
-static_assert(WT_W1 % 16 == 0, "aligned operand blocks");
+static_assert(WT_B1 % 16 == 0 && WT_BW % 16 == 0 && WT_XL + 128 * KX * 2 <= WT_B, "aligned operand blocks");
 
 // features of predicted entry q of system s (zeros past the last one)
 __device__ __forceinline__ void warm_features(const DevPattern& P, int s, int q, const double* __restrict__ A,
@@ -625,18 +629,18 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
   __shared__ double s_num[WARM_THREADS / 32], s_den[WARM_THREADS / 32];
   __shared__ int s_ok, s_fail;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // weights: W2 as the K-major B operand (row u = output unit, k = input unit), W1 / b1 as float4 x 3 per
-  // hidden unit, (b2, w3) pairs
+  // weights: W2 as the K-major B operand of layer 2 (row u = output unit, k = input unit), W1 | b1 as the
+  // K-major B operand of layer 1 (row v: W1[v][0..8], b1[v], zeros), (b2, w3) pairs
   {
     const uint4* w2g = reinterpret_cast<const uint4*>(pbf + OW2);  // row u: 8 chunks of 8 BF16
     for (int k = tid; k < H * 8; k += WARM_THREADS) {
       const int u = k >> 3, c = k & 7;
       *reinterpret_cast<uint4*>(smraw + WT_B + tc::kmajor_off(u, 8 * c, H)) = w2g[k];
     }
-    float* w1 = reinterpret_cast<float*>(smraw + WT_W1);
-    for (int k = tid; k < H * 12; k += WARM_THREADS) {
-      const int v = k / 12, c = k % 12;
-      w1[k] = c < NF ? __bfloat162float(pbf[OW1 + v * NF + c]) : (c == NF ? __bfloat162float(pbf[OB1 + v]) : 0.0f);
+    for (int k = tid; k < H * KX; k += WARM_THREADS) {
+      const int v = k / KX, c = k % KX;
+      const __nv_bfloat16 w = c < NF ? pbf[OW1 + v * NF + c] : (c == NF ? pbf[OB1 + v] : __float2bfloat16_rn(0.0f));
+      *reinterpret_cast<__nv_bfloat16*>(smraw + WT_B1 + tc::kmajor_off(v, c, KX)) = w;
     }
     float2* bw = reinterpret_cast<float2*>(smraw + WT_BW);
     for (int u = tid; u < H; u += WARM_THREADS) bw[u] = make_float2(__bfloat162float(pbf[OB2 + u]), __bfloat162float(pbf[OW3 + u]));
@@ -651,55 +655,85 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = s_tmem;
-  const float4* w1v = reinterpret_cast<const float4*>(smraw + WT_W1);
   const float2* bw = reinterpret_cast<const float2*>(smraw + WT_BW);
   const float b3 = __bfloat162float(pbf[OB3]);
   const uint32_t a_hi = tc::smem_u32(smraw + WT_AH), a_lo = tc::smem_u32(smraw + WT_AL);
-  const uint32_t b_w2 = tc::smem_u32(smraw + WT_B);
-  constexpr uint32_t kSbo = H * 16;  // K = 64: 8-row groups 1024 bytes apart
+  const uint32_t x_hi = tc::smem_u32(smraw + WT_XH), x_lo = tc::smem_u32(smraw + WT_XL);
+  const uint32_t b_w2 = tc::smem_u32(smraw + WT_B), b_w1 = tc::smem_u32(smraw + WT_B1);
+  constexpr uint32_t kSbo = H * 16, kSboX = KX * 16;  // 8-row groups 1024 / 256 bytes apart
   const uint32_t idesc = tc::idesc_bf16(128, H);
   const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's 32 TMEM lanes
   const int ntile = (P.n_mlp + WARM_THREADS - 1) / WARM_THREADS;
   uint32_t phase = 0;
+  // one tensor-core round: wait (bounded) for the MMAs committed last, then make the accumulator readable;
+  // false (uniformly) when the round did not complete
+  auto round_done = [&]() {
+    const bool done = tc::mbar_wait(&s_mbar, phase, kWaitLimit);
+    phase ^= 1u;
+    if (!done) s_fail = 1;
+    tc::fence_after_sync();
+    __syncthreads();
+    return s_fail == 0;
+  };
   for (int s = blockIdx.x; s < nsys; s += gridDim.x) {
     const double* As = A + (size_t)s * P.nnz;
     double* Ls = LU0 + (size_t)s * P.nnz;
     for (int e = tid; e < P.nnz; e += WARM_THREADS) Ls[e] = As[e];
     const bool failed = s_fail != 0;  // uniform: written before the last barrier
     float f[NF];
-    double ab;
-    int e;
+    double ab = 0.0;
+    int e = -1;
     if (!failed) warm_features(P, s, tid, A, rown, coln, corr, f, ab, e);
     __syncthreads();  // the copy of A is complete before any prediction overwrites it
     for (int tile = 0; tile < ntile && !failed; ++tile) {
-      // layer 1 on the CUDA cores, 8 hidden units at a time into one 16-byte chunk of each A operand
-#pragma unroll 1
-      for (int c = 0; c < H / 8; ++c) {
-        uint32_t hi[4], lo[4];
+      // ---- layer 1: this entry's features (and 1.0 for the bias) as row tid of the K = 16 operand
+      {
+        __align__(16) __nv_bfloat16 hi[KX], lo[KX];
 #pragma unroll
-        for (int d = 0; d < 8; d += 2) {
-          float h2[2];
-#pragma unroll
-          for (int x = 0; x < 2; ++x) {
-            const int v = 8 * c + d + x;
-            const float4 wa = w1v[v * 3], wb = w1v[v * 3 + 1], wc = w1v[v * 3 + 2];
-            const float w[NF] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w, wc.x};
-            float pa = wc.y;  // b1
-#pragma unroll
-            for (int k = 0; k < NF; ++k) pa = fmaf(w[k], f[k], pa);
-            h2[x] = gelu_fast(pa);
-          }
-          const float h0 = __bfloat162float(__float2bfloat16_rn(h2[0]));
-          const float h1 = __bfloat162float(__float2bfloat16_rn(h2[1]));
-          hi[d >> 1] = pack_bf16(h0, h1);
-          lo[d >> 1] = pack_bf16(h2[0] - h0, h2[1] - h1);
+        for (int k = 0; k < KX; ++k) {
+          const float x = k < NF ? f[k] : (k == NF ? 1.0f : 0.0f);
+          hi[k] = __float2bfloat16_rn(x);
+          lo[k] = __float2bfloat16_rn(x - __bfloat162float(hi[k]));
         }
-        const uint32_t off = tc::kmajor_off(tid, 8 * c, H);
-        *reinterpret_cast<uint4*>(smraw + WT_AH + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<uint4*>(smraw + WT_AL + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+#pragma unroll
+        for (int c = 0; c < KX / 8; ++c) {
+          const uint32_t off = tc::kmajor_off(tid, 8 * c, KX);
+          *reinterpret_cast<uint4*>(smraw + WT_XH + off) = reinterpret_cast<const uint4*>(hi)[c];
+          *reinterpret_cast<uint4*>(smraw + WT_XL + off) = reinterpret_cast<const uint4*>(lo)[c];
+        }
       }
-      // the operands (generic-proxy stores) become visible to the tensor core, and every thread's
-      // previous accumulator reads are done, before one thread issues layer 2
+      tc::fence_smem_to_async();
+      tc::fence_before_sync();  // every thread's previous accumulator reads are done
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        tc::mma_bf16(tmem, tc::sdesc(x_hi, kSboX), tc::sdesc(b_w1, kSboX), idesc, 0);
+        tc::mma_bf16(tmem, tc::sdesc(x_lo, kSboX), tc::sdesc(b_w1, kSboX), idesc, 1);
+        tc::commit(&s_mbar);
+      }
+      if (!round_done()) break;
+      // ---- GELU of this row of pre1 into the layer-2 operands (hi and lo), 16 units at a time
+#pragma unroll 1
+      for (int c = 0; c < H / 16; ++c) {
+        float acc[16];
+        tc::ld16(trow + 16 * c, acc);
+        uint32_t hi[8], lo[8];
+#pragma unroll
+        for (int d = 0; d < 16; d += 2) {
+          const float h0 = gelu_fast(acc[d]), h1 = gelu_fast(acc[d + 1]);
+          const float g0 = __bfloat162float(__float2bfloat16_rn(h0));
+          const float g1 = __bfloat162float(__float2bfloat16_rn(h1));
+          hi[d >> 1] = pack_bf16(g0, g1);
+          lo[d >> 1] = pack_bf16(h0 - g0, h1 - g1);
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const uint32_t off = tc::kmajor_off(tid, 16 * c + 8 * q, H);
+          *reinterpret_cast<uint4*>(smraw + WT_AH + off) = make_uint4(hi[4 * q], hi[4 * q + 1], hi[4 * q + 2], hi[4 * q + 3]);
+          *reinterpret_cast<uint4*>(smraw + WT_AL + off) = make_uint4(lo[4 * q], lo[4 * q + 1], lo[4 * q + 2], lo[4 * q + 3]);
+        }
+      }
+      // ---- layer 2
       tc::fence_smem_to_async();
       tc::fence_before_sync();
       __syncthreads();
@@ -717,13 +751,8 @@ __global__ void __launch_bounds__(WARM_THREADS) k_mlp_warm(const DevPattern P, i
       const double ab_cur = ab;
       const int e_cur = e;
       if (tile + 1 < ntile) warm_features(P, s, (tile + 1) * WARM_THREADS + tid, A, rown, coln, corr, f, ab, e);
-      const bool done = tc::mbar_wait(&s_mbar, phase, kWaitLimit);
-      phase ^= 1u;
-      if (!done) s_fail = 1;
-      tc::fence_after_sync();
-      __syncthreads();
-      if (s_fail) break;  // uniform
-      // this thread's row of the accumulator: b2, GELU, output layer
+      if (!round_done()) break;
+      // ---- this thread's row of pre2: b2, GELU, output layer
       float out = 0.0f;
 #pragma unroll 1
       for (int c = 0; c < H / 16; ++c) {
