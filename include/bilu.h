@@ -299,7 +299,9 @@ bilu_status bilu_true_residual(const bilu_plan* plan, int nsys, const double* d_
  * n <= 128, 256, 512, 1024, larger (5 buckets), each run as one persistent
  * kernel over a work queue (largest systems first); in BILU_REDUCE_FAST order
  * n <= 64, 96, 128, 192, 256, 384, 512, 768, 1024, larger (10 buckets), those
- * with n <= 1024 run as one register-resident CTA per system (largest first).
+ * with n <= 1024 run the register-resident solver, one CTA per system (largest
+ * first) or a persistent grid over the bucket's work queue, whichever the
+ * autotuner measures faster.
  * A solve replays one CUDA graph holding every bucket launch on concurrent
  * branches.  The graph is captured on the first solve and again whenever the
  * device pointers change. */
@@ -307,17 +309,31 @@ typedef struct bilu_uneven_plan bilu_uneven_plan;
 bilu_status bilu_uneven_plan_create(bilu_uneven_plan** plan, int nsys, const int* h_sys_n, const int* h_sys_nnz,
                                     const int* h_row_ptrs, const int* h_col_idxs, const bilu_options* opts);
 bilu_status bilu_uneven_plan_destroy(bilu_uneven_plan* plan);
-/* Times every candidate CTA size per bucket on the given batch and keeps the
- * fastest: 64..1024 threads with the persistent grid from the occupancy of
- * each, or, for register-resident buckets, 1x, 2x and 4x the fewest threads.
+/* Tunes every bucket's CTA size and grid on the given batch: persistent
+ * shared-memory buckets time 64..1024 threads (grid from the occupancy of
+ * each) on the bucket alone; register-resident buckets, largest systems
+ * first, try 1x, 2x and 4x the fewest threads, each with one CTA per system
+ * and with a persistent grid over the bucket's work queue, judged by the time
+ * of the whole graph-launched batch (the buckets run concurrently there).
  * Synchronises the stream; overwrites d_x. */
 bilu_status bilu_uneven_autotune(bilu_uneven_plan* plan, const double* d_values, const double* d_b, double* d_x,
                                  void* stream);
 bilu_status bilu_uneven_solve(bilu_uneven_plan* plan, const double* d_values, const double* d_b, double* d_x,
                               const bilu_results* results, void* stream);
+/* Pins bucket `bucket`'s CTA size (threads, 0 = keep) and grid (0 = one CTA
+ * per system for register-resident buckets, the occupancy-sized persistent
+ * grid otherwise; a smaller grid makes the bucket's CTAs persistent over its
+ * work queue), instead of (or after) the autotuner's choice.  The results do
+ * not depend on the grid; for register-resident buckets the CTA size is part
+ * of the FAST order.  BILU_ERR_INVALID when the CTA size does not fit.  No
+ * reference counterpart. */
+bilu_status bilu_uneven_set_config(bilu_uneven_plan* plan, int bucket, int threads, int grid);
 /* Bucket `bucket` (0 .. count - 1; BILU_ERR_INVALID past the last one): n
- * range (n_lo, n_hi], systems, chosen CTA size, grid, shared memory per CTA,
- * autotuned time (ms, -1 if not tuned). */
+ * range (n_lo, n_hi], systems, chosen CTA size, grid (below `systems`:
+ * persistent CTAs over the bucket's work queue), shared memory per CTA,
+ * autotuned time (ms, -1 if not tuned; the bucket alone for persistent
+ * shared-memory buckets, the whole batch after this bucket's choice for
+ * register-resident ones). */
 bilu_status bilu_uneven_get_info(const bilu_uneven_plan* plan, int bucket, int* n_lo, int* n_hi, int* systems,
                                  int* threads, int* grid, int* smem_bytes, float* tuned_ms);
 

@@ -33,7 +33,7 @@ EXPORTED = [
     "bilu_version", "bilu_device_count", "bilu_gen_stencil", "bilu_gen_stencil_range", "bilu_gen_uneven",
     "bilu_plan_enable_timing",
     "bilu_plan_last_timing", "bilu_plan_autotune", "bilu_solve_noalloc", "bilu_uneven_plan_create", "bilu_uneven_plan_destroy",
-    "bilu_uneven_autotune", "bilu_uneven_solve", "bilu_uneven_get_info", "bilu_forward_error",
+    "bilu_uneven_autotune", "bilu_uneven_solve", "bilu_uneven_get_info", "bilu_uneven_set_config", "bilu_forward_error",
     "bilu_mlp_create", "bilu_mlp_destroy", "bilu_mlp_param_count", "bilu_mlp_get_params", "bilu_mlp_set_params",
     "bilu_mlp_train", "bilu_mlp_loss_grad", "bilu_mlp_eval", "bilu_mlp_warm_start", "bilu_mlp_save", "bilu_mlp_load",
     "bilu_probe_fp64_rate",
@@ -106,6 +106,7 @@ def lib():
         L.bilu_uneven_autotune.argtypes = [vp, vp, vp, vp, vp]
         L.bilu_uneven_solve.argtypes = [vp, vp, vp, vp, C.POINTER(Results), vp]
         L.bilu_uneven_get_info.argtypes = [vp, i, ip, ip, ip, ip, ip, ip, C.POINTER(C.c_float)]
+        L.bilu_uneven_set_config.argtypes = [vp, i, i, i]
         L.bilu_forward_error.argtypes = [vp, i, ip, vp, vp, vp, C.POINTER(d), vp, vp]
         fp = C.POINTER(C.c_float)
         L.bilu_mlp_create.argtypes = [C.POINTER(vp), C.c_uint64]
@@ -247,6 +248,11 @@ class UnevenPlan:
         R = Results(*(C.c_void_p(t.data_ptr()) if t is not None else None
                       for t in (iters, conv, res, true_res, status)))
         _check(lib().bilu_uneven_solve(self.h, _dev(values), _dev(b), _dev(x), C.byref(R), _stream(stream)))
+
+    def set_config(self, bucket, threads=0, grid=0):
+        """Pins a bucket's CTA size and grid (bilu_uneven_set_config; grid below the bucket's systems: persistent
+        CTAs over its work queue)."""
+        _check(lib().bilu_uneven_set_config(self.h, bucket, threads, grid))
 
     def info(self):
         """Per size bucket: n range, systems, CTA size, grid, shared memory, autotuned time."""

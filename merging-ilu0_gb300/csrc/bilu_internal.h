@@ -291,10 +291,12 @@ struct UnevenArgs {
 };
 
 // kernel launch wrappers (k_solve.cu / k_factor.cu)
-// register-resident solver over one uneven-batch bucket: CTA b solves system
-// order[b] with nt threads, R rows per thread (pv 0 none, 3 merged ILU(0))
+// register-resident solver over one uneven-batch bucket with nt threads, R rows
+// per thread (pv 0 none, 3 merged ILU(0)): CTA b solves system order[b]
+// (grid = the bucket's systems), or a persistent grid of fewer CTAs takes the
+// systems from the bucket's work queue (u.counter, zeroed before the launch)
 const void* rr_uneven_kernel(int pv, int fp32, int R);
-cudaError_t launch_uneven_rr(const UnevenArgs& u, int nt, int R, int pv, int fp32, cudaStream_t st);
+cudaError_t launch_uneven_rr(const UnevenArgs& u, int nt, int R, int pv, int fp32, int grid, cudaStream_t st);
 void* uneven_kernel(int fp32, int reduce_fast, int maxl);
 cudaError_t launch_uneven(const UnevenArgs& u, int threads, int grid, int fp32, int reduce_fast, int maxl,
                           cudaStream_t st);

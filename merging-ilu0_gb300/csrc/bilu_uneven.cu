@@ -9,8 +9,9 @@
 // longest first.  In the reference operation order each bucket runs as one
 // persistent kernel whose CTAs take systems from an atomic work queue; in FAST
 // order, buckets of systems with n <= 1024 run the register-resident solver,
-// one CTA per system.  The per-bucket CTA size (and persistent grid) come from
-// an autotuner that times the candidates on the caller's batch.  All bucket
+// either one CTA per system or as a persistent grid over the bucket's work
+// queue.  The per-bucket CTA size and grid come from an autotuner that times
+// the candidates on the caller's batch.  All bucket
 // launches (and the zeroing of the queue heads) are captured once into a CUDA
 // graph whose branches run concurrently; a solve is one graph launch.
 #include <cuda_runtime.h>
@@ -37,8 +38,9 @@ struct Bucket {
   int grid = 0;              // persistent CTAs
   float tuned_ms = -1.0f;
   int maxn = 0;
-  bool rr = false;           // register-resident solver, one CTA per system (FAST order, n <= 1024)
+  bool rr = false;           // register-resident solver (FAST order, n <= 1024)
   int R = 0;                 // its rows per thread
+  int rr_occ = 0;            // its resident CTAs per SM (the persistent grid is rr_occ x SMs)
   int rr_rest = 0;           // its largest layout without the reduction slot (which depends on the CTA size)
 };
 
@@ -123,8 +125,14 @@ bool rr_setup(const bilu_uneven_plan* U, Bucket& b, int nt) {
   b.rr = true;
   b.R = R;
   b.threads = nt;
+  b.rr_occ = occ;
   b.grid = (int)b.sys.size();
   return true;
+}
+
+// The persistent grid of a register-resident bucket: every resident CTA slot, at most one per system.
+int rr_persistent_grid(const bilu_uneven_plan* U, const Bucket& b) {
+  return std::min((int)b.sys.size(), b.rr_occ * U->nsm);
 }
 
 int occupancy_grid(const bilu_uneven_plan* U, const Bucket& b, int threads) {
@@ -148,7 +156,8 @@ bilu_status launch_bucket(bilu_uneven_plan* U, int bi, const double* vals, const
   const Bucket& b = U->buckets[bi];
   if (b.sys.empty()) return BILU_OK;
   const UnevenArgs u = make_args(U, b, bi, vals, rhs, x, R);
-  cudaError_t e = b.rr ? launch_uneven_rr(u, b.threads, b.R, rr_pv(U->opts), U->opts.factor_precision == BILU_FP32, st)
+  cudaError_t e = b.rr ? launch_uneven_rr(u, b.threads, b.R, rr_pv(U->opts), U->opts.factor_precision == BILU_FP32,
+                                          b.grid, st)
                        : launch_uneven(u, b.threads, b.grid, U->opts.factor_precision == BILU_FP32,
                                        U->opts.reduction == BILU_REDUCE_FAST, b.maxl, st);
   return e == cudaSuccess ? BILU_OK : cuda_fail(e, "uneven launch");
@@ -455,26 +464,18 @@ bilu_status bilu_uneven_autotune(bilu_uneven_plan* U, const double* d_values, co
   cudaEventCreate(&e1);
   const int cands[] = {64, 128, 256, 512, 1024};
   bilu_status res = BILU_OK;
+  // Persistent shared-memory buckets (reference order): each CTA size timed on the bucket alone.
   for (int bi = 0; bi < (int)U->buckets.size() && !res; ++bi) {
     Bucket& b = U->buckets[bi];
-    if (b.sys.empty()) continue;
+    if (b.sys.empty() || b.rr) continue;
     int best_t = b.threads, best_g = b.grid;
     float best = 1e30f;
-    const int rr_base = round32((b.maxn + 7) / 8);
-    const int rr_cands[] = {rr_base, 2 * rr_base, 4 * rr_base, 0, 0};
-    for (int ci = 0; ci < 5; ++ci) {
-      const int t = b.rr ? rr_cands[ci] : cands[ci];
-      if (t <= 0) continue;
+    for (int t : cands) {
+      const int g = occupancy_grid(U, b, t);
+      if (g <= 0) continue;
       Bucket trial = b;
-      if (b.rr) {
-        if (!rr_setup(U, trial, t)) continue;
-      } else {
-        const int g = occupancy_grid(U, b, t);
-        if (g <= 0) continue;
-        trial.threads = t;
-        trial.grid = g;
-      }
-      const int g = trial.grid;
+      trial.threads = t;
+      trial.grid = g;
       std::swap(U->buckets[bi], trial);
       float ms_min = 1e30f;
       for (int rep = 0; rep < 2 && !res; ++rep) {
@@ -495,13 +496,65 @@ bilu_status bilu_uneven_autotune(bilu_uneven_plan* U, const double* d_values, co
         best_g = g;
       }
     }
-    if (b.rr) {
-      rr_setup(U, b, best_t);  // threads, rows per thread, grid and shared memory of the winner
-    } else {
-      b.threads = best_t;
-      b.grid = best_g;
-    }
+    b.threads = best_t;
+    b.grid = best_g;
     b.tuned_ms = best;
+  }
+  // Register-resident buckets (FAST order): the bucket launches run concurrently in the solve's graph, so a
+  // bucket's configuration is judged by the whole graph-launched batch, not by the bucket alone.  Measured
+  // on GB300 with the 8192-system benchmark batch: timed alone, the persistent grid won for four of nine
+  // buckets and larger CTAs for several, and together those choices made the batch slower than the
+  // untuned plan.  One greedy pass over the buckets, largest systems first: each tries 1x, 2x and 4x the
+  // fewest threads, each with one CTA per system and with the persistent grid over its work queue, and
+  // keeps whatever makes the whole batch fastest (best of three graph launches per candidate).
+  auto whole = [&](float* out) -> bilu_status {
+    bilu_status r = capture(U, d_values, d_b, d_x, nullptr);
+    float best_ms = 1e30f;
+    for (int rep = 0; rep < 3 && !r; ++rep) {
+      cudaEventRecord(e0, st);
+      cudaError_t ce = cudaGraphLaunch(U->exec, st);
+      cudaEventRecord(e1, st);
+      if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+      if (ce != cudaSuccess) r = cuda_fail(ce, "autotune graph launch");
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best_ms = std::min(best_ms, ms);
+    }
+    *out = best_ms;
+    return r;
+  };
+  bool any_rr = false;
+  for (const Bucket& b : U->buckets) any_rr = any_rr || (b.rr && !b.sys.empty());
+  float base = 0.0f;
+  if (any_rr && !res) res = whole(&base);
+  for (int bi = (int)U->buckets.size() - 1; bi >= 0 && any_rr && !res; --bi) {
+    Bucket& b = U->buckets[bi];
+    if (!b.rr || b.sys.empty()) continue;
+    const Bucket keep = b;
+    Bucket best_cfg = b;
+    const int rr_base = round32((b.maxn + 7) / 8);
+    for (int f : {1, 2, 4}) {
+      Bucket trial = keep;
+      if (!rr_setup(U, trial, f * rr_base)) continue;
+      const int pgrid = rr_persistent_grid(U, trial);
+      for (int g : {trial.grid, pgrid}) {
+        if (g == pgrid && pgrid >= trial.grid) continue;  // the persistent grid is one CTA per system anyway
+        if (f * rr_base == keep.threads && g == keep.grid) continue;  // the configuration already timed
+        Bucket cfg = trial;
+        cfg.grid = g;
+        b = cfg;
+        float ms = 0.0f;
+        res = whole(&ms);
+        if (res) break;
+        if (ms < base) {
+          base = ms;
+          best_cfg = cfg;
+        }
+      }
+      if (res) break;
+    }
+    b = best_cfg;
+    b.tuned_ms = base;  // the whole batch with this bucket's choice
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -523,6 +576,33 @@ bilu_status bilu_uneven_solve(bilu_uneven_plan* U, const double* d_values, const
   }
   cudaError_t e = cudaGraphLaunch(U->exec, (cudaStream_t)stream);
   return e == cudaSuccess ? BILU_OK : cuda_fail(e, "cudaGraphLaunch");
+}
+
+bilu_status bilu_uneven_set_config(bilu_uneven_plan* U, int bucket, int threads, int grid) {
+  if (!U) return set_error(BILU_ERR_INVALID, "bilu_uneven_set_config: NULL plan");
+  if (bucket < 0 || bucket >= (int)U->buckets.size()) return set_error(BILU_ERR_INVALID, "bucket out of range");
+  if (threads < 0 || grid < 0) return set_error(BILU_ERR_INVALID, "bilu_uneven_set_config: negative size");
+  Bucket& b = U->buckets[bucket];
+  if (b.sys.empty()) return BILU_OK;
+  const int count = (int)b.sys.size();
+  if (b.rr) {
+    Bucket trial = b;
+    if (!rr_setup(U, trial, threads > 0 ? threads : b.threads))
+      return set_error(BILU_ERR_INVALID, "bilu_uneven_set_config: " + std::to_string(threads) +
+                                             " threads do not fit this bucket's register-resident solver");
+    trial.grid = grid > 0 ? std::min(grid, count) : count;
+    b = trial;
+  } else {
+    const int t = threads > 0 ? threads : b.threads;
+    const int g = occupancy_grid(U, b, t);
+    if (t % 32 || t > 1024 || g <= 0)
+      return set_error(BILU_ERR_INVALID, "bilu_uneven_set_config: " + std::to_string(t) + " threads do not fit");
+    b.threads = t;
+    b.grid = grid > 0 ? std::min(grid, g) : g;
+  }
+  b.tuned_ms = -1.0f;
+  drop_graph(U);  // the captured graph used the previous configuration
+  return BILU_OK;
 }
 
 bilu_status bilu_uneven_get_info(const bilu_uneven_plan* U, int bucket, int* n_lo, int* n_hi, int* systems,

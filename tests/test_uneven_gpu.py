@@ -1,8 +1,8 @@
 """Uneven batches (own size and pattern per system): one graph-launched solve
 of size-bucketed kernels, checked per system against the oracle bit for bit,
 in the reference operation order (persistent shared-memory kernels) and in
-FAST order (the register-resident solver, one CTA per system, its bucket's
-threads per system)."""
+FAST order (the register-resident solver with its bucket's threads per system,
+one CTA per system or persistent over the bucket's work queue)."""
 import numpy as np
 import pytest
 
@@ -114,6 +114,35 @@ def test_uneven_fast_bitwise(cuda, fp32):
     assert np.all(g["conv"] == 1)
     assert np.all(g["res"] < 1e-10 * bn)
     assert np.all(g["true_res"] < 1e-8 * bn)
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_uneven_fast_persistent_queue_bitwise(cuda, fp32):
+    """Register-resident buckets as persistent grids over their work queues (bilu_uneven_set_config with 1 to
+    3 CTAs, so every CTA takes several systems from the queue) give the same bits as the oracle; a second
+    solve on the same buffers replays the captured graph, whose queue heads it zeroes itself."""
+    import torch
+    sn, sz, rp, ci, v, b = bilu.gen_uneven(40, seed=13, nmin=16, nmax=700)
+    tol = dict(tol_mode=bilu.TOL_REL, tol=1e-10)
+    with bilu.UnevenPlan(sn, sz, rp, ci, reduction=bilu.REDUCE_FAST,
+                         factor_precision=bilu.FP32 if fp32 else bilu.FP64, **tol) as plan:
+        for k, i in enumerate(plan.info()):
+            if i["systems"] > 1:
+                plan.set_config(k, 0, 1 + k % 3)
+        info = plan.info()
+        assert any(0 < i["grid"] < i["systems"] for i in info)
+        g, bufs = _run(cuda, plan, v, b, len(sn))
+        V, B, X, it, cv, rs, tr, st = bufs
+        for t, fill in ((X, float("nan")), (it, -7.0), (cv, 7), (rs, -1.0), (tr, -1.0), (st, 99)):
+            t.fill_(fill)
+        plan.solve(V, B, X, it, cv, rs, tr, st)
+        torch.cuda.synchronize()
+        g2 = {"x": X.cpu().numpy(), "iters": it.cpu().numpy(), "conv": cv.cpu().numpy(), "res": rs.cpu().numpy(),
+              "true_res": tr.cpu().numpy(), "status": st.cpu().numpy()}
+    want = _oracle_uneven_fast(sn, sz, rp, ci, v, b, info, fp32, **tol)
+    _cmp(g, want, f"uneven FAST persistent fp32={fp32}")
+    _cmp(g2, want, f"uneven FAST persistent replay fp32={fp32}")
+    assert np.all(g["conv"] == 1)
 
 
 def test_uneven_fast_unpreconditioned_bitwise(cuda):
