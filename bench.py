@@ -52,45 +52,45 @@ SECONDARY = [
     dict(name="parilu5_isai_3d7_10x10x10_fp64", kind=2, grid=(10, 10, 10), nsys=4096, autotune=True,
          desc="headline workload with FP64 ISAI values",
          opts=dict(precond=4, parilu_sweeps=5, isai_power=2, tol_mode=1, tol=1e-10, reduction=1, factor_precision=0)),
-    dict(name="plain_ilu0_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096,
+    dict(name="plain_ilu0_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096, autotune=True,
          desc="plain form on the headline systems: merged FP64 ILU(0) BiCGSTAB, FAST order (register-resident "
               "kernel: ILU(0) and the factors in shared memory, vectors in registers)",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1)),
-    dict(name="fp32_ilu0_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096,
+    dict(name="fp32_ilu0_3d7_10x10x10", kind=2, grid=(10, 10, 10), nsys=4096, autotune=True,
          desc="headline systems, merged ILU(0) with the factors stored and applied in FP32 (FP64 factorisation, "
               "A*x, inner products, recurrences), FAST order",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1), fwd_sample=32),
-    dict(name="plain_ilu0_2d5_16x16_fast", kind=1, grid=(16, 16, 1), nsys=16384,
+    dict(name="plain_ilu0_2d5_16x16_fast", kind=1, grid=(16, 16, 1), nsys=16384, autotune=True,
          desc="plain form: merged FP64 ILU(0) BiCGSTAB, 16384 FP64 systems, 2D 5-point 16x16, rel 1e-10, FAST order "
               "(register-resident kernel)",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1)),
-    dict(name="fp32_ilu0_2d5_16x16", kind=1, grid=(16, 16, 1), nsys=16384,
+    dict(name="fp32_ilu0_2d5_16x16", kind=1, grid=(16, 16, 1), nsys=16384, autotune=True,
          desc="16384 2D 5-point 16x16 systems, merged ILU(0) with FP32-stored factors, FAST order",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1)),
     dict(name="fp32_isai_2d5_16x16", kind=1, grid=(16, 16, 1), nsys=16384, autotune=True,
          desc="16384 2D 5-point 16x16 systems, ILU(0) + ISAI stored and applied in FP32 (FP64 A*x, inner products, "
               "recurrences), FAST order",
          opts=dict(precond=3, ilu_approach=3, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1)),
-    dict(name="plain_ilu0_2d5_16x16_ref", kind=1, grid=(16, 16, 1), nsys=16384,
+    dict(name="plain_ilu0_2d5_16x16_ref", kind=1, grid=(16, 16, 1), nsys=16384, autotune=True,
          desc="plain form in the reference's operation order (bit-identical iterates; register-resident one-warp "
               "kernel)",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=0)),
-    dict(name="ref_rule_merged_ilu0_2d5_16x16_ref", kind=1, grid=(16, 16, 1), nsys=16384,
+    dict(name="ref_rule_merged_ilu0_2d5_16x16_ref", kind=1, grid=(16, 16, 1), nsys=16384, autotune=True,
          desc="the reference merged kernel's workload and stopping rule (absolute 1e-11 on the recursive residual, "
               "500 iterations): merged FP64 ILU(0) BiCGSTAB of 16384 2D 5-point 16x16 systems in the reference's "
               "operation order (bit-identical to the reference kernel)",
          opts=dict(precond=0, tol_mode=0, tol=1e-11, reduction=0)),
-    dict(name="ref_rule_merged_ilu0_2d5_16x16_fast", kind=1, grid=(16, 16, 1), nsys=16384,
+    dict(name="ref_rule_merged_ilu0_2d5_16x16_fast", kind=1, grid=(16, 16, 1), nsys=16384, autotune=True,
          desc="the same batch and stopping rule in FAST order (register-resident kernel)",
          opts=dict(precond=0, tol_mode=0, tol=1e-11, reduction=1)),
     dict(name="fp32_isai_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768, autotune=True,
          desc="ILU(0) + ISAI stored and applied in FP32 (FP64 A*x, inner products, recurrences), 32768 "
               "convection-diffusion systems 24x24",
          opts=dict(precond=3, ilu_approach=3, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1), fwd_sample=256),
-    dict(name="fp32_ilu0_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768,
+    dict(name="fp32_ilu0_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768, autotune=True,
          desc="FP32-stored ILU(0) factors (FP64 recurrences), 32768 convection-diffusion systems 24x24",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=1), fwd_sample=256),
-    dict(name="fp64_ilu0_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768,
+    dict(name="fp64_ilu0_cd2d_24x24", kind=4, grid=(24, 24, 1), nsys=32768, autotune=True,
          desc="same workload with FP64 factors",
          opts=dict(precond=0, tol_mode=1, tol=1e-10, reduction=1, factor_precision=0), fwd_sample=256),
 ]

@@ -110,10 +110,11 @@ typedef struct bilu_options {
                                 Bit 3: A and aiU left in global memory are read from
                                 SELL-32 copies made before the solver launch (same
                                 arithmetic; the copies live in the plan's workspace).
-                                Bit 4: the kernel variant with 4 CTAs of 128 threads per
-                                SM (128 registers per thread instead of 168; same
-                                arithmetic), taken for 8 rows per thread without ILU
-                                factors and ignored otherwise.                            */
+                                Bit 4: the kernel variant bounded for occupancy (same
+                                arithmetic, fewer registers, more threads per SM): 8 rows
+                                per thread on 4 CTAs of 128 threads per SM, 4 rows on 4
+                                CTAs of 256 (3 with ILU factors), 2 rows on 2 CTAs of
+                                512; ignored for ILU factors at 8 rows per thread.        */
 } bilu_options;
 
 /* Fills *opts with the reference defaults: merged ILU(0), approach 1, 5 sweeps,
@@ -164,7 +165,7 @@ typedef struct bilu_plan_info {
   int operands_in_smem;  /* bit 0: A, bit 1: factors / aiL, bit 2: aiU in shared memory;
                             bit 3: A, and aiU, left in global memory are read from SELL-32
                             copies made by one extra launch each per solve; bit 4: the
-                            4-CTAs-per-SM variant of the register-resident kernel */
+                            occupancy variant of the register-resident kernel */
   int solver_kernel;     /* 0: one CTA per system, vectors in shared memory (every mode);
                             1: register-resident (BILU_REDUCE_FAST with n <= 1024, or
                             the reference order with n <= 1024, ILU factors or none and

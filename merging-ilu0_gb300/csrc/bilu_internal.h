@@ -306,6 +306,8 @@ cudaError_t launch_solve(const SolveArgs& a, int threads, int fp32, int reduce_f
 int rr_rows_per_thread(int n, int nt);  // smallest R in {1, 2, 4, 8} with R * nt >= n, else 0
 int rr_max_threads(int R);
 const void* rr_kernel(int pv, int fp32, int R, int ref, int occ4);  // null: no such variant
+// the occupancy variant (k_bicgstab_rr_occ, k_solve_rr_occ.cu) for R rows per thread; null: none
+const void* rr_occ_kernel(int pv, int fp32, int R);
 cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, int ref, int occ4,
                             cudaStream_t st);
 size_t solve_max_smem();

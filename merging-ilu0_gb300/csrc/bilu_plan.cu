@@ -393,10 +393,11 @@ void choose_layout(bilu_plan& P) {
 // and the shared-memory staging `mask` (bit 0 A, bit 1 aiL / aiA, bit 2 aiU;
 // operands that would cost occupancy are left in global memory, read through
 // L1; ILU factors are always staged; bit 3: the SpMVs read SELL-32 copies of
-// the operands left in global memory; bit 4: the kernel variant with 4 CTAs of
-// 128 threads per SM, taken for 8 rows per thread without ILU factors and
-// otherwise ignored); false when the kernel does not apply or that
-// configuration is invalid.
+// the operands left in global memory; bit 4: the occupancy variant of the
+// kernel (k_bicgstab_rr_occ: 8 rows per thread on 4 CTAs of 128 threads, 4 rows
+// on 4 CTAs of 256 (3 with ILU factors), 2 rows on 2 CTAs of 512; ignored for
+// ILU factors at 8 rows per thread); false when the kernel does not apply or
+// that configuration is invalid.
 bool rr_configure(bilu_plan& P, int nt, int mask) {
   const bilu_options& o = P.opts;
   const int pk = prec_kind(o.precond);
@@ -415,7 +416,10 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
     if ((pv != 0 && pv != 3) || P.a_maxl > 16) return false;
     mask &= 7;
   }
-  const bool occ4 = (mask & 16) != 0 && R == 8 && pv != 3;
+  // bit 4: the occupancy variant, for 2, 4 or 8 rows per thread (ILU factors: 2 or 4) and at most its
+  // launch bound of threads
+  const int occ_nt = R == 8 ? 128 : (R == 4 ? 256 : 512);
+  const bool occ4 = (mask & 16) != 0 && (R == 2 || R == 4 || (R == 8 && pv != 3)) && nt <= occ_nt;
   const bool fp32 = is_fp32(o);
   const int fts = fp32 ? 4 : 8;
   if (pv == 3 && P.tp_lo.empty()) return false;
@@ -923,7 +927,8 @@ bilu_status bilu_plan_autotune(bilu_plan* P, int nsys, const double* d_values, c
   int best_nt = keep_nt, best_mask = -1;
   for (int f : {1, 2, 4}) {
     for (int mask : {0, 2, 6, 1, 8, 10, 14, 16, 18, 22, 24, 26}) {
-      if ((mask & 16) && (rr_rows_per_thread(P->n, base * f) != 8 || P->rr_pv == 3)) continue;  // bit 4 ignored
+      const int rf = rr_rows_per_thread(P->n, base * f);
+      if ((mask & 16) && (rf < 2 || (rf == 8 && P->rr_pv == 3))) continue;  // bit 4 ignored
       if ((mask & 24) && P->opts.reduction != BILU_REDUCE_FAST) continue;                         // bits 3, 4 ignored
       if (!rr_configure(*P, base * f, mask)) continue;
       float ms = 0.0f;

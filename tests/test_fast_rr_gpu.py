@@ -67,22 +67,23 @@ HEADLINE_OPTS = dict(precond=bilu.PRECOND_PARILU0_ISAI, parilu_sweeps=5, isai_po
                      factor_precision=bilu.FP32, max_iter=500, **TOL)
 
 
-@pytest.mark.parametrize("staging", [16, 6, 0])
-def test_headline_configuration_bitwise(cuda, staging):
+@pytest.mark.parametrize("threads,staging", [(128, 16), (128, 6), (128, 0), (256, 16)])
+def test_headline_configuration_bitwise(cuda, threads, staging):
     """The benchmark's headline path (PrecondBiCGSTAB_ilu_isai_gpu.cu:267-339: ParILU, ISAI of L and U, solver)
     on 16 systems of its 3D 7-point 10x10x10 pattern: ParILU(0) 5 sweeps (k_parilu0, FAST), ISAI computed in
     FP32 (k_isai_f32), 128 threads with 8 rows each.  Staging 16 is the configuration the autotuner picks for
     the 4096-system headline on GB300: the 4-CTA-per-SM kernel (k_bicgstab_rr_occ4, 128 registers, four
     block reductions of 4 warps) with every operand read through L1; 6 stages aiL and aiU in shared memory
-    (3 CTAs per SM), 0 stages nothing.  x, iterations, status, both norms and the true residual equal the
-    oracle's FAST order bit for bit."""
+    (3 CTAs per SM), 0 stages nothing; 256 threads with staging 16 run the 4-CTA variant with 4 rows per
+    thread (k_bicgstab_rr_occ4_r4, 64 registers).  x, iterations, status, both norms and the true residual
+    equal the oracle's FAST order bit for bit."""
     rp, ci, v, b = H.workload("3d7_10x10x10", 16)
-    g = H.gpu_solve(cuda, rp, ci, v, b, smem_staging=staging, threads_per_system=128, **HEADLINE_OPTS)
+    g = H.gpu_solve(cuda, rp, ci, v, b, smem_staging=staging, threads_per_system=threads, **HEADLINE_OPTS)
     info = g["info"]
-    assert info["threads"] == 128
+    assert info["threads"] == threads
     assert bool(info["operands_in_smem"] & 16) == (staging == 16), info
-    o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_PARILU0_ISAI, 128, True, **TOL)
-    _check(g, o, f"headline 3D 10x10x10 ParILU(5)+FP32 ISAI, staging {staging}")
+    o = _oracle_fast(rp, ci, v, b, bilu.PRECOND_PARILU0_ISAI, threads, True, **TOL)
+    _check(g, o, f"headline 3D 10x10x10 ParILU(5)+FP32 ISAI, {threads} threads, staging {staging}")
     assert np.all(g["conv"] == 1) and np.all(g["status"] == bilu.SYS_CONVERGED)
 
 
@@ -284,6 +285,35 @@ def test_rr_four_ctas_per_sm_bitwise(cuda, precond, kw, fp32):
     o = _oracle_fast(rp, ci, v, b, precond, g["info"]["threads"], fp32, sweeps=kw.get("parilu_sweeps", 5),
                      power=kw.get("isai_power", 2), **TOL)
     _check(g, o, f"4 CTAs per SM, precond {precond} fp32={fp32}")
+    assert np.all(g["conv"] == 1)
+
+
+OCC_CASES = [
+    ("3d7_10x10x10", bilu.PRECOND_ILU0, dict(ilu_approach=1), 256),        # ILU factors, 4 rows per thread
+    ("2d5_16x16", bilu.PRECOND_ILU0, dict(ilu_approach=1), 128),           # ILU factors, 2 rows per thread
+    ("cd2d_24x24", bilu.PRECOND_ILU0_SPLIT, dict(ilu_approach=3), 192),    # given factors, 4 rows per thread
+    ("3d7_7x7x7", bilu.PRECOND_PARILU0_ISAI, dict(parilu_sweeps=5), 128),  # ISAI, 4 rows per thread
+    ("3d7_7x7x7", bilu.PRECOND_GENERAL_ISAI, dict(isai_power=2), 256),     # general ISAI, 2 rows per thread
+    ("2d5_16x16", bilu.PRECOND_NONE, {}, 128),                             # none, 2 rows per thread
+]
+
+
+@pytest.mark.parametrize("fam,precond,kw,nt", OCC_CASES,
+                         ids=[f"{c[0]}-p{c[1]}-t{c[3]}" for c in OCC_CASES])
+@pytest.mark.parametrize("fp32", [False, True])
+def test_rr_occupancy_variants_bitwise(cuda, fam, precond, kw, nt, fp32):
+    """The occupancy variants of the register-resident kernel (staging bit 4, k_bicgstab_rr_occ: fewer
+    registers, more threads per SM) at 2 and 4 rows per thread, for ILU factors (in-kernel and given), ISAI
+    and no preconditioner: the same bits as the oracle's FAST order for that thread count."""
+    if precond == bilu.PRECOND_NONE and fp32:
+        pytest.skip("no preconditioner values to round")
+    rp, ci, v, b = H.workload(fam, NSYS)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, reduction=bilu.REDUCE_FAST, smem_staging=16,
+                    threads_per_system=nt, factor_precision=bilu.FP32 if fp32 else bilu.FP64, **kw, **TOL)
+    assert g["info"]["threads"] == nt and g["info"]["operands_in_smem"] & 16, g["info"]
+    o = _oracle_fast(rp, ci, v, b, precond, nt, fp32, approach=kw.get("ilu_approach", 1),
+                     sweeps=kw.get("parilu_sweeps", 5), power=kw.get("isai_power", 2), **TOL)
+    _check(g, o, f"occupancy variant {fam} precond {precond} threads {nt} fp32={fp32}")
     assert np.all(g["conv"] == 1)
 
 
