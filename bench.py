@@ -96,15 +96,14 @@ SECONDARY = [
 ]
 
 
-# DRAM bytes (read + write) of one register-resident solver launch on the headline workload, per
-# system, in the configuration the autotuner chooses there (the 4-CTA-per-SM variant, operands read
-# through L1: smem_staging 16): ncu dram__bytes_read.sum + dram__bytes_write.sum of a 3072-system
-# launch (430.4 + 38.0 MB) / 3072; the traffic grows in proportion to the systems of a launch.
-RR_TRAFFIC_BYTES_PER_SYSTEM = 152_460
-# the same capture's FP64-pipe figure, sm__pipe_fp64_cycles_active (percent of peak sustained elapsed)
-RR_NCU = {"kernel": "k_bicgstab_rr_occ4<1, float>", "sm__pipe_fp64_cycles_active_pct": 53.8,
-          "dram_bytes_per_system": RR_TRAFFIC_BYTES_PER_SYSTEM,
-          "source": "profiles/k_bicgstab_rr_occ4_parilu5_isai_fp32_3d7_10x10x10.md (3072 systems)"}
+# ncu figures of one register-resident solver launch on the headline workload in the configuration the
+# autotuner chooses there on GB300 (the occupancy variant with 4 rows per thread: 256 threads per system,
+# 4 CTAs per SM, operands read through L1; smem_staging 16): DRAM bytes (dram__bytes_read.sum +
+# dram__bytes_write.sum) of a 3072-system launch divided by 3072 -- the traffic grows in proportion to the
+# systems of a launch -- and the FP64 pipe (sm__pipe_fp64_cycles_active, percent of peak sustained active).
+RR_NCU = {"kernel": "k_bicgstab_rr_occ<4, 1, float>", "threads_per_system": 256, "smem_staging": 16,
+          "sm__pipe_fp64_cycles_active_pct": 68.5, "dram_bytes_per_system": 189_580,
+          "source": "profiles/k_bicgstab_rr_occ_parilu5_isai_fp32_3d7_10x10x10.md (3072 systems)"}
 
 # systems of the headline workload that both CPU timings run (the GPU line's cpu_baseline and every step of
 # --impl reference): the whole 4096-system batch, so that the two samples are the same work
@@ -123,6 +122,19 @@ def fp64_flops_per_iter(n, nnz, prec_nnz, precond):
     fma = 2 * nnz + 6 * n + 6 * n
     fma += 2 * prec_nnz
     return 2 * fma
+
+
+def solver_kernel_name(info, n, opts):
+    """The solver kernel a plan launches, from its configuration (bilu_plan_get_info)."""
+    if info["solver_kernel"] != 1:
+        return "k_bicgstab (shared-memory solver)"
+    rows = next(r for r in (1, 2, 4, 8) if r * info["threads"] >= n)
+    pv = {0: 3, 1: 3, 2: 3, 3: 1, 4: 1, 5: 0, 6: 2}[opts["precond"]]
+    ft = "float" if opts.get("factor_precision", 0) == 1 and pv else "double"
+    if info["operands_in_smem"] & 16:
+        return f"k_bicgstab_rr_occ<{rows}, {pv}, {ft}> (register-resident solver, occupancy variant, " \
+               f"{info['threads']} threads per system)"
+    return f"k_bicgstab_rr<{rows}, {pv}, {ft}> (register-resident solver, {info['threads']} threads per system)"
 
 
 def launches_per_step(info):
@@ -540,6 +552,19 @@ def measure_learned(dev, stream, ntrain=65536, neval=16384, train_steps=1500, ba
     out = {"name": "learned_warm_start_3d7_7x7x7", "ntrain": ntrain, "neval": neval, "train_steps": train_steps,
            "batch": batch, "train_s": train_s, "loss_first": float(losses[:10].mean()),
            "loss_last": float(losses[-10:].mean())}
+    # inference alone: the warm start of all evaluation systems (both layers on the tensor cores)
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            m.warm_start(plan, V2, LU0, 1e-3, res, used, stream=stream)
+        torch.cuda.synchronize()
+        w0, w1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0.record(stream)
+        for _ in range(steps):
+            m.warm_start(plan, V2, LU0, 1e-3, res, used, stream=stream)
+        w1.record(stream)
+        torch.cuda.synchronize()
+    out["warm_start_ms"] = w0.elapsed_time(w1) / steps
+    out["train_ms_per_step"] = 1e3 * train_s / train_steps
     with torch.cuda.stream(stream):
         for mode in ("plain", "learned"):
             def step():
@@ -604,6 +629,8 @@ def main():
     ap.add_argument("--smem-staging", type=int, default=-1,
                     help="with --no-autotune: the solver configuration mask (bilu_options.smem_staging), e.g. the "
                          "one the autotuner chooses, so that a profiling run launches that kernel")
+    ap.add_argument("--threads", type=int, default=0,
+                    help="with --no-autotune: threads per system of the solver (profiling runs)")
     ap.add_argument("--workload", default="",
                     help="with --kernel-only: measure this secondary workload (by name) instead of the headline "
                          "(profiling runs)")
@@ -620,6 +647,10 @@ def main():
         if not args.no_autotune:
             ap.error("--smem-staging needs --no-autotune")
         HEADLINE["opts"] = dict(HEADLINE["opts"], smem_staging=args.smem_staging)
+    if args.threads > 0:
+        if not args.no_autotune:
+            ap.error("--threads needs --no-autotune")
+        HEADLINE["opts"] = dict(HEADLINE["opts"], threads_per_system=args.threads)
     if args.nsys > 0:
         HEADLINE["desc"] = HEADLINE["desc"].replace(f"{HEADLINE['nsys']} FP64", f"{args.nsys} FP64")
         HEADLINE["nsys"] = args.nsys
@@ -751,9 +782,10 @@ def main():
     flops = fp64_flops_per_iter(n, nnz, prec_nnz, HEADLINE["opts"]["precond"]) * res["mean_iters"] * nsys
     host = cpu_info()
     rate, dt, used, _ = cpu_port_rate(HEADLINE, CPU_SAMPLE)
-    kernel = (("k_bicgstab_rr_occ4 (register-resident solver, 4 CTAs per SM)" if info["operands_in_smem"] & 16
-               else "k_bicgstab_rr (register-resident solver)") if info["solver_kernel"] == 1 else "k_bicgstab (solver)")
-    autotuned_occ4 = info["solver_kernel"] == 1 and fp32_prec and bool(info["operands_in_smem"] & 16)
+    kernel = solver_kernel_name(info, n, HEADLINE["opts"])
+    # the ncu figures hold for the configuration they were captured in
+    captured = (info["solver_kernel"] == 1 and fp32_prec and info["threads"] == RR_NCU["threads_per_system"]
+                and info["operands_in_smem"] == RR_NCU["smem_staging"])
     line = {
         "metric": METRIC, "value": value, "unit": "systems/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -766,7 +798,8 @@ def main():
         "e2e": res["e2e"],
         "gpu_launches": launches_per_step(info) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": RR_TRAFFIC_BYTES_PER_SYSTEM * nsys if autotuned_occ4 else None,
+                     "traffic": RR_NCU["dram_bytes_per_system"] * nsys
+                     if captured and RR_NCU["dram_bytes_per_system"] else None,
                      "traffic_source": RR_NCU["source"] + ", scaled per system", "peak_kind": peak_kind,
                      "kernel": kernel, "bytes_per_system": bps,
                      "achieved_from": "bytes_per_system x nsys / the solver launch's CUDA-event time (stages_ms.solve)"},
@@ -777,7 +810,7 @@ def main():
                           "peak_sm_mhz": fp64_probe_mhz,
                           "counted": "FP64 operations of the BiCGSTAB iterations (bench.fp64_flops_per_iter x mean "
                                      "iterations x systems); FP32 ISAI work not counted",
-                          "ncu": RR_NCU if autotuned_occ4 else None,
+                          "ncu": RR_NCU if captured else None,
                           "note": "FP64 issue, not HBM, bounds this kernel on GB300"},
         "stages_ms": {"setup": res["setup_ms"], "solve": res["solve_ms"]},
         "solve_quality": {"mean_iters": res["mean_iters"], "max_iters": res["max_iters"],
