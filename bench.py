@@ -635,12 +635,16 @@ def main():
                     help="with --kernel-only: measure this secondary workload (by name) instead of the headline "
                          "(profiling runs)")
     args = ap.parse_args()
-    if args.workload:
+    learned_only = args.workload == "learned_warm_start_3d7_7x7x7"
+    if args.workload and not learned_only:
         found = [w for w in SECONDARY if w["name"] == args.workload]
         if not found or not args.kernel_only:
-            ap.error("--workload needs --kernel-only and one of: " + ", ".join(w["name"] for w in SECONDARY))
+            ap.error("--workload needs --kernel-only and one of: " + ", ".join(
+                [w["name"] for w in SECONDARY] + ["learned_warm_start_3d7_7x7x7"]))
         HEADLINE.clear()
         HEADLINE.update(found[0])
+    if learned_only and not args.kernel_only:
+        ap.error("--workload learned_warm_start_3d7_7x7x7 needs --kernel-only")
     if args.no_autotune:
         HEADLINE["autotune"] = False
     if args.smem_staging >= 0:
@@ -676,6 +680,10 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
+    if learned_only:  # profiling runs of the learned warm start: training, inference, the solves
+        if rank == 0:
+            print(json.dumps(measure_learned(dev, stream, steps=args.steps)))
+        return
     sampler = ClockSampler(local)
     import shard
     first, _ = shard.slab(HEADLINE["nsys"] * world, rank, world)  # B systems per rank (weak scaling)
