@@ -282,3 +282,14 @@ def test_dense_lu_bitwise_and_forward_error(cuda, family):
     ref = np.linalg.norm(g["x"][ids] - xd, axis=1) / np.linalg.norm(xd, axis=1)
     np.testing.assert_allclose(fe, ref, rtol=1e-12, atol=1e-30)
     assert np.all(fe < 1e-8)
+
+
+def test_fp64_rate_probe(cuda):
+    """bilu_probe_fp64_rate, the FP64 roofline's peak in the benchmark: a positive DFMA rate below the
+    part's nominal FP64 figure (2 lane-FMAs per clock per SM), with the SM clock it ran at."""
+    import torch
+    gflops, mhz = bilu.probe_fp64_rate()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert 100.0 < mhz < 4000.0
+    assert 0.0 < gflops <= 2 * 2 * sms * mhz * 1e-3 * 1.02
+
