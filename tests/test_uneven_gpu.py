@@ -145,6 +145,24 @@ def test_uneven_fast_persistent_queue_bitwise(cuda, fp32):
     assert np.all(g["conv"] == 1)
 
 
+def test_uneven_set_config_rejects_bad_configurations(cuda):
+    """bilu_uneven_set_config: buckets out of range, negative sizes and CTA sizes the register-resident solver
+    cannot take (more than 8 rows per thread, not a multiple of 32) are errors that leave the plan usable."""
+    sn, sz, rp, ci, v, b = bilu.gen_uneven(24, seed=3, nmin=16, nmax=1000)
+    with bilu.UnevenPlan(sn, sz, rp, ci, reduction=bilu.REDUCE_FAST, tol_mode=bilu.TOL_REL, tol=1e-10) as plan:
+        info = plan.info()
+        k = max(i for i, x in enumerate(info) if x["systems"])
+        bad = [(len(info), 0, 0), (-1, 0, 0), (k, -32, 0), (k, 0, -1), (k, 33, 0)]
+        if info[k]["n_lo"] >= 256:
+            bad.append((k, 32, 0))  # more than 8 rows per thread
+        for args in bad:
+            with pytest.raises(bilu.BiluError) as e:
+                plan.set_config(*args)
+            assert e.value.code == bilu.ERR_INVALID, args
+        g, _ = _run(cuda, plan, v, b, len(sn))
+        assert np.all(g["conv"] == 1)
+
+
 def test_uneven_fast_unpreconditioned_bitwise(cuda):
     sn, sz, rp, ci, v, b = bilu.gen_uneven(24, seed=4, nmin=16, nmax=400)
     tol = dict(tol_mode=bilu.TOL_ABS, tol=1e-11, max_iter=60)
