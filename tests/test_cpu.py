@@ -3,6 +3,7 @@ logic (generators, pattern validation), and the oracle's own consistency."""
 import ctypes
 import os
 import re
+import sys
 
 import numpy as np
 import pytest
@@ -205,6 +206,13 @@ def test_bench_reference_arm_json_line(built):
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    # the same workload as the GPU arm's line: its config key for key, the same dtype, the same CPU sample
+    sys.path.insert(0, ROOT)
+    import bench
+    assert line["config"] == bench.headline_config(1)
+    assert line["dtype"] == bench.headline_dtype() == "f64 (ISAI FP32)"
+    assert str(bench.CPU_SAMPLE) in cb["sample"] and cb["host"]["nproc"] >= 1 and cb["host"]["model"]
+    assert "reference_gpu_kernels" in line
 
 
 def test_oracle_pipeline_pattern_cache_keeps_results(built):
@@ -218,3 +226,22 @@ def test_oracle_pipeline_pattern_cache_keeps_results(built):
     assert set(cache) == {"diag", "split", "isai_l", "isai_u"}
     for k in ("x", "iters", "res", "true_res", "ail", "aiu"):
         H.assert_bitwise(got[k], want[k], k)
+
+
+def test_bench_names_the_solver_kernel_from_the_plan(built):
+    """bench.solver_kernel_name reads the plan's configuration: rows per thread from n and the CTA size, the
+    occupancy variant from staging bit 4, the preconditioner values' type."""
+    sys.path.insert(0, ROOT)
+    import bench
+    isai32 = dict(precond=4, factor_precision=1)
+    info = dict(solver_kernel=1, threads=256, operands_in_smem=16)
+    assert bench.solver_kernel_name(info, 1000, isai32).startswith("k_bicgstab_rr_occ<4, 1, float>")
+    info = dict(solver_kernel=1, threads=128, operands_in_smem=6)
+    assert bench.solver_kernel_name(info, 1000, isai32).startswith("k_bicgstab_rr<8, 1, float>")
+    assert bench.solver_kernel_name(dict(solver_kernel=1, threads=32, operands_in_smem=0), 256,
+                                    dict(precond=0)).startswith("k_bicgstab_rr<8, 3, double>")
+    assert bench.solver_kernel_name(dict(solver_kernel=0, threads=1024, operands_in_smem=0), 1000,
+                                    isai32).startswith("k_bicgstab ")
+    assert bench.launches_per_step(dict(operands_in_smem=16)) == 3
+    assert bench.launches_per_step(dict(operands_in_smem=8)) == 5
+
