@@ -302,13 +302,14 @@ cudaError_t launch_uneven(const UnevenArgs& u, int threads, int grid, int fp32, 
                           cudaStream_t st);
 cudaError_t launch_solve(const SolveArgs& a, int threads, int fp32, int reduce_fast, int maxl, cudaStream_t st);
 // register-resident solver: pv 0 none, 1 ISAI of L and U, 2 general ISAI, 3 ILU factors;
-// ref: the reference's operation order; occ4: the 4-CTAs-per-SM variant (R = 8, pv != 3)
+// ref: the reference's operation order; occ: the occupancy variant (k_bicgstab_rr_occ: R = 2, 4, 8;
+// ILU factors at R = 2, 4)
 int rr_rows_per_thread(int n, int nt);  // smallest R in {1, 2, 4, 8} with R * nt >= n, else 0
 int rr_max_threads(int R);
-const void* rr_kernel(int pv, int fp32, int R, int ref, int occ4);  // null: no such variant
+const void* rr_kernel(int pv, int fp32, int R, int ref, int occ);  // null: no such variant
 // the occupancy variant (k_bicgstab_rr_occ, k_solve_rr_occ.cu) for R rows per thread; null: none
 const void* rr_occ_kernel(int pv, int fp32, int R);
-cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, int ref, int occ4,
+cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, int ref, int occ,
                             cudaStream_t st);
 size_t solve_max_smem();
 cudaError_t launch_expand(const DevPattern& p, int nsys, const double* vin, double* vout, cudaStream_t st);
@@ -397,7 +398,7 @@ struct bilu_plan {
   bool rr = false;
   int rr_threads = 0, rr_pv = 0;
   bool rr_sell = false;  // SpMVs read SELL-32 copies of A (and of aiU) made before the solver launch
-  bool rr_occ4 = false;  // the 4-CTAs-per-SM kernel variant (staging bit 4)
+  bool rr_occ = false;  // the 4-CTAs-per-SM kernel variant (staging bit 4)
   bilu::RRLayout rr_lay;
   // workspace
   void* ws = nullptr;

@@ -419,7 +419,7 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   // bit 4: the occupancy variant, for 2, 4 or 8 rows per thread (ILU factors: 2 or 4) and at most its
   // launch bound of threads
   const int occ_nt = R == 8 ? 128 : (R == 4 ? 256 : 512);
-  const bool occ4 = (mask & 16) != 0 && (R == 2 || R == 4 || (R == 8 && pv != 3)) && nt <= occ_nt;
+  const bool occ_variant = (mask & 16) != 0 && (R == 2 || R == 4 || (R == 8 && pv != 3)) && nt <= occ_nt;
   const bool fp32 = is_fp32(o);
   const int fts = fp32 ? 4 : 8;
   if (pv == 3 && P.tp_lo.empty()) return false;
@@ -435,7 +435,7 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const void* k = rr_kernel(pv, fp32 ? 1 : 0, R, ref ? 1 : 0, occ4 ? 1 : 0);
+  const void* k = rr_kernel(pv, fp32 ? 1 : 0, R, ref ? 1 : 0, occ_variant ? 1 : 0);
   if (!k) return false;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(optin, off)) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, nt, off) != cudaSuccess || occ < 1) {
@@ -456,7 +456,7 @@ bool rr_configure(bilu_plan& P, int nt, int mask) {
   P.rr_pv = pv;
   P.rr_lay = L;
   P.rr_sell = (mask & 8) != 0 && !P.sa_off.empty();
-  P.rr_occ4 = occ4;
+  P.rr_occ = occ_variant;
   return true;
 }
 
@@ -922,7 +922,7 @@ bilu_status bilu_plan_autotune(bilu_plan* P, int nsys, const double* d_values, c
   const int base = round_up((P->n + 7) / 8, 32);
   const int keep_nt = P->rr_threads;
   const RRLayout keep_lay = P->rr_lay;
-  const bool keep_sell = P->rr_sell, keep_occ4 = P->rr_occ4;
+  const bool keep_sell = P->rr_sell, keep_occ = P->rr_occ;
   float best = -1.0f;
   int best_nt = keep_nt, best_mask = -1;
   for (int f : {1, 2, 4}) {
@@ -955,7 +955,7 @@ bilu_status bilu_plan_autotune(bilu_plan* P, int nsys, const double* d_values, c
     P->rr_threads = keep_nt;
     P->rr_lay = keep_lay;
     P->rr_sell = keep_sell;
-    P->rr_occ4 = keep_occ4;
+    P->rr_occ = keep_occ;
   }
   P->timing = had_timing;
   return st;
@@ -993,7 +993,7 @@ bilu_status bilu_plan_get_info(const bilu_plan* P, bilu_plan_info* info) {
     info->threads = P->rr_threads;
     info->smem_bytes = P->rr_lay.total;
     info->operands_in_smem = (P->rr_lay.A >= 0 ? 1 : 0) | (P->rr_lay.ail >= 0 ? 2 : 0) | (P->rr_lay.aiu >= 0 ? 4 : 0) |
-                             (P->rr_sell ? 8 : 0) | (P->rr_occ4 ? 16 : 0);
+                             (P->rr_sell ? 8 : 0) | (P->rr_occ ? 16 : 0);
   }
   return BILU_OK;
 }
@@ -1160,7 +1160,7 @@ bilu_status solve_launch(bilu_plan* P, int nsys, const double* vals, const doubl
     a.A_sell = (const double*)(ws + sc.asell);
   }
   e = P->rr ? launch_solve_rr(a, P->rr_lay, P->rr_threads, P->rr_pv, fp32 ? 1 : 0,
-                              o.reduction == BILU_REDUCE_FAST ? 0 : 1, P->rr_occ4 ? 1 : 0, st)
+                              o.reduction == BILU_REDUCE_FAST ? 0 : 1, P->rr_occ ? 1 : 0, st)
             : launch_solve(a, P->threads, fp32 ? 1 : 0, o.reduction == BILU_REDUCE_FAST ? 1 : 0, maxl, st);
   if (e != cudaSuccess) return cuda_err(e, "solver launch");
   if (P->timing) cudaEventRecord(P->ev[2], st);

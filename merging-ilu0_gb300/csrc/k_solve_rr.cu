@@ -42,8 +42,8 @@ int rr_rows_per_thread(int n, int nt) {
 
 int rr_max_threads(int R) { return R <= 1 ? 1024 : (R == 2 ? 512 : (R == 4 ? 256 : 128)); }
 
-const void* rr_kernel(int pv, int fp32, int R, int ref, int occ4) {
-  if (occ4) {  // FAST order, the occupancy variants (R = 2, 4, 8; ILU factors at R = 2, 4)
+const void* rr_kernel(int pv, int fp32, int R, int ref, int occ) {
+  if (occ) {  // FAST order, the occupancy variants (R = 2, 4, 8; ILU factors at R = 2, 4)
     if (ref || (R != 2 && R != 4 && R != 8) || (R == 8 && pv == 3)) return nullptr;
     return rr_occ_kernel(pv, fp32, R);
   }
@@ -58,12 +58,12 @@ const void* rr_kernel(int pv, int fp32, int R, int ref, int occ4) {
   return fp32 ? rr_kernel_pv<2, float, false>(R) : rr_kernel_pv<2, double, false>(R);
 }
 
-cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, int ref, int occ4,
+cudaError_t launch_solve_rr(const SolveArgs& a, const RRLayout& L, int nt, int pv, int fp32, int ref, int occ,
                             cudaStream_t st) {
   if (a.nsys == 0) return cudaSuccess;
   const int R = rr_rows_per_thread(a.pat.n, nt);
   if (R == 0 || nt % 32 || nt > rr_max_threads(R)) return cudaErrorInvalidConfiguration;
-  const void* k = rr_kernel(pv, fp32, R, ref, occ4);
+  const void* k = rr_kernel(pv, fp32, R, ref, occ);
   if (!k) return cudaErrorInvalidConfiguration;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total);
   if (e != cudaSuccess) return e;

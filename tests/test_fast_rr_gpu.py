@@ -71,12 +71,12 @@ HEADLINE_OPTS = dict(precond=bilu.PRECOND_PARILU0_ISAI, parilu_sweeps=5, isai_po
 def test_headline_configuration_bitwise(cuda, threads, staging):
     """The benchmark's headline path (PrecondBiCGSTAB_ilu_isai_gpu.cu:267-339: ParILU, ISAI of L and U, solver)
     on 16 systems of its 3D 7-point 10x10x10 pattern: ParILU(0) 5 sweeps (k_parilu0, FAST), ISAI computed in
-    FP32 (k_isai_f32), 128 threads with 8 rows each.  Staging 16 is the configuration the autotuner picks for
-    the 4096-system headline on GB300: the 4-CTA-per-SM kernel (k_bicgstab_rr_occ4, 128 registers, four
-    block reductions of 4 warps) with every operand read through L1; 6 stages aiL and aiU in shared memory
-    (3 CTAs per SM), 0 stages nothing; 256 threads with staging 16 run the 4-CTA variant with 4 rows per
-    thread (k_bicgstab_rr_occ4_r4, 64 registers).  x, iterations, status, both norms and the true residual
-    equal the oracle's FAST order bit for bit."""
+    FP32 (k_isai_f32), then the solver.  256 threads with staging 16 is the configuration the autotuner picks
+    for the 4096-system headline on GB300: the occupancy variant with 4 rows per thread
+    (k_bicgstab_rr_occ<4, 1, float>, 4 CTAs of 256 threads per SM, 64 registers) with every operand read
+    through L1.  With 128 threads (8 rows each): staging 16 runs k_bicgstab_rr_occ<8, 1, float> (4 CTAs, 128
+    registers), 6 stages aiL and aiU in shared memory (3 CTAs per SM), 0 stages nothing.  x, iterations,
+    status, both norms and the true residual equal the oracle's FAST order bit for bit."""
     rp, ci, v, b = H.workload("3d7_10x10x10", 16)
     g = H.gpu_solve(cuda, rp, ci, v, b, smem_staging=staging, threads_per_system=threads, **HEADLINE_OPTS)
     info = g["info"]
