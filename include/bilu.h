@@ -406,6 +406,15 @@ int bilu_device_count(void);
  * Allocates 32 bytes and synchronises the stream.  No reference counterpart. */
 bilu_status bilu_probe_fp64_rate(double* h_gflops, double* h_sm_mhz, void* stream);
 
+/* Checks the FP64 <-> FP32 conversions the FP32 preconditioner paths use (round
+ * to nearest even by integer operations, the hardware conversion for float
+ * subnormal results, infinities and NaNs) against the hardware conversions on
+ * n_per_thread bit patterns per thread of 4 CTAs of 256 threads per SM: random
+ * doubles, doubles across every float exponent boundary with rounding ties,
+ * and random floats.  h_mismatch[0] / [1]: roundings / widenings that differ
+ * (0 and 0 expected).  Synchronises the stream.  No reference counterpart. */
+bilu_status bilu_check_conversions(int n_per_thread, uint64_t seed, unsigned long long* h_mismatch, void* stream);
+
 /* ---------------------------------------------------------------- synthetic inputs */
 /* Seeded generators of the benchmark workloads (host memory; no GPU needed).
  * kind: 1 = 2D 5-point (gx*gy), diag 4+U(0,1), off -(1+0.2U(-1,1)), E/W skew +-0.3U(0,1);

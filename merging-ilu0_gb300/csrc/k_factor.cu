@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "bilu_internal.h"
+#include "k_cvt.cuh"
 
 namespace bilu {
 namespace {
@@ -326,7 +327,7 @@ __global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, 
   float* LU = reinterpret_cast<float*>(smem);
   float* M = LU + nnz;                                                  // max(ail_nnz, aiu_nnz)
   float* rinv = M + (P.ail_nnz > P.aiu_nnz ? P.ail_nnz : P.aiu_nnz);  // n
-  for (int k = threadIdx.x; k < nnz; k += blockDim.x) LU[k] = (float)__ldg(LUg + (size_t)sys * nnz + k);
+  for (int k = threadIdx.x; k < nnz; k += blockDim.x) LU[k] = cvt::f32(__ldg(LUg + (size_t)sys * nnz + k));
   __syncthreads();
   // ---- aiL (unit diagonal)
   for (int i = threadIdx.x; i < n; i += blockDim.x) {

@@ -64,6 +64,7 @@
 #include <cuda_runtime.h>
 
 #include "bilu_internal.h"
+#include "k_cvt.cuh"
 
 namespace bilu {
 namespace {
@@ -153,6 +154,26 @@ __device__ __forceinline__ bool ref_chain_sum(double (&v)[K], Term term, double*
 
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+// FP64 -> FT and FT -> FP64 with the integer conversions for float (k_cvt.cuh).
+// Used where the conversions share the SMs with FP64 work (the ISAI paths:
+// preconditioner input and output around the FP32 SpMVs).  The level-scheduled
+// triangular solves keep the hardware conversions: those phases issue no FP64
+// arithmetic, and the integer form only adds latency there (measured 1-2 %
+// slower on the FP32-factor paths).
+template <typename FT>
+__device__ __forceinline__ FT round_t(double x) {
+  if constexpr (sizeof(FT) == 4)
+    return cvt::f32(x);
+  else
+    return x;
+}
+template <typename FT>
+__device__ __forceinline__ double widen_t(FT y) {
+  if constexpr (sizeof(FT) == 4)
+    return cvt::f64(y);
+  else
+    return y;
+}
 
 // out[k] = row (tid + k*nt) of M times xv, for the R rows of this thread
 // (rows >= n give 0).  The R rows advance together, entry j of every row per
@@ -508,7 +529,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
         rows_acc<R>(AIU, uci, P.aiu_rp, rb, rs, n, smid, z_);                                              \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
         const int i = rb + k * rs;                                                                              \
-        if (i < n) sph[i] = (double)z_[k];                                                                       \
+        if (i < n) sph[i] = widen_t(z_[k]);                                                                      \
       }                                                                                                          \
       __syncthreads();                                                                                           \
     } else if (PV == 2) {                                                                                        \
@@ -516,7 +537,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
       rows_acc<R>(AIL, lci, P.ail_rp, rb, rs, n, sin, z_);                                                 \
       _Pragma("unroll") for (int k = 0; k < R; ++k) {                                                            \
         const int i = rb + k * rs;                                                                              \
-        if (i < n) sph[i] = (double)z_[k];                                                                       \
+        if (i < n) sph[i] = widen_t(z_[k]);                                                                      \
       }                                                                                                          \
       __syncthreads();                                                                                           \
     } else if (PV == 3) {                                                                                        \
@@ -532,7 +553,7 @@ __device__ __forceinline__ void rr_solve(const SolveArgs& a, const DevPattern& P
         if (PV == 0 || (PV == 3 && sizeof(FT) == 8)) \
           sph[i] = vec[k];                       \
         else                                     \
-          sin[i] = (FT)vec[k];                   \
+          sin[i] = PV == 3 ? (FT)vec[k] : round_t<FT>(vec[k]); \
       }                                          \
     }                                            \
   } while (0)

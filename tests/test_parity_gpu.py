@@ -293,3 +293,11 @@ def test_fp64_rate_probe(cuda):
     assert 100.0 < mhz < 4000.0
     assert 0.0 < gflops <= 2 * 2 * sms * mhz * 1e-3 * 1.02
 
+
+
+def test_integer_conversions_match_hardware(cuda):
+    """The FP32 preconditioner paths round and widen with integer operations (k_cvt.cuh) and leave float
+    subnormal results, infinities and NaNs to the hardware: every bit equal to the hardware conversions on
+    about 160 million patterns of each kind (random doubles, every float exponent boundary with rounding
+    ties, random floats)."""
+    assert bilu.check_conversions(1024, seed=7) == (0, 0)
