@@ -406,14 +406,18 @@ int bilu_device_count(void);
  * Allocates 32 bytes and synchronises the stream.  No reference counterpart. */
 bilu_status bilu_probe_fp64_rate(double* h_gflops, double* h_sm_mhz, void* stream);
 
-/* Checks the FP64 <-> FP32 conversions the FP32 preconditioner paths use (round
- * to nearest even by integer operations, the hardware conversion for float
- * subnormal results, infinities and NaNs) against the hardware conversions on
- * n_per_thread bit patterns per thread of 4 CTAs of 256 threads per SM: random
- * doubles, doubles across every float exponent boundary with rounding ties,
- * and random floats.  h_mismatch[0] / [1]: roundings / widenings that differ
- * (0 and 0 expected).  Synchronises the stream.  No reference counterpart. */
-bilu_status bilu_check_conversions(int n_per_thread, uint64_t seed, unsigned long long* h_mismatch, void* stream);
+/* Checks the FP64 operations the kernels do with integer arithmetic against
+ * the hardware: the FP64 <-> FP32 conversions of the FP32 preconditioner paths
+ * (round to nearest even; the hardware conversion for float subnormal results,
+ * infinities and NaNs) and the correctly rounded FP64 reciprocal of the FAST
+ * ParILU and ISAI (against __drcp_rn; the hardware's for zero, subnormal,
+ * infinite and NaN inputs and subnormal results), on n_per_thread bit patterns
+ * per thread of 4 CTAs of 256 threads per SM: random doubles, doubles across
+ * every float exponent boundary with rounding ties, random floats, and
+ * doubles with short, long and zero mantissas.  h_mismatch[0] / [1] / [2]:
+ * roundings / widenings / reciprocals that differ (0, 0, 0 expected).
+ * Synchronises the stream.  No reference counterpart. */
+bilu_status bilu_check_integer_fp(int n_per_thread, uint64_t seed, unsigned long long* h_mismatch, void* stream);
 
 /* ---------------------------------------------------------------- synthetic inputs */
 /* Seeded generators of the benchmark workloads (host memory; no GPU needed).

@@ -37,7 +37,7 @@ EXPORTED = [
     "bilu_mlp_create", "bilu_mlp_destroy", "bilu_mlp_param_count", "bilu_mlp_get_params", "bilu_mlp_set_params",
     "bilu_mlp_train", "bilu_mlp_loss_grad", "bilu_mlp_eval", "bilu_mlp_warm_start", "bilu_mlp_save", "bilu_mlp_load",
     "bilu_probe_fp64_rate",
-    "bilu_check_conversions",
+    "bilu_check_integer_fp",
 ]
 
 
@@ -122,7 +122,7 @@ def lib():
         L.bilu_mlp_save.argtypes = [vp, C.c_char_p]
         L.bilu_mlp_load.argtypes = [vp, C.c_char_p]
         L.bilu_probe_fp64_rate.argtypes = [C.POINTER(d), C.POINTER(d), vp]
-        L.bilu_check_conversions.argtypes = [i, C.c_uint64, C.POINTER(C.c_ulonglong), vp]
+        L.bilu_check_integer_fp.argtypes = [i, C.c_uint64, C.POINTER(C.c_ulonglong), vp]
         L.bilu_plan_enable_timing.argtypes = [vp, i]
         L.bilu_plan_last_timing.argtypes = [vp, C.POINTER(Timing)]
         L.bilu_gen_uneven.argtypes = [i, C.c_uint64, i, i, i, i, ip, ip, ip, ip, C.POINTER(d), C.POINTER(d)]
@@ -182,12 +182,12 @@ def probe_fp64_rate(stream=None):
     return g.value, m.value
 
 
-def check_conversions(n_per_thread=1024, seed=1, stream=None):
-    """(roundings, widenings) of the kernels' integer FP64 <-> FP32 conversions that differ from the hardware's
-    on n_per_thread bit patterns per thread; bilu_check_conversions."""
-    out = (C.c_ulonglong * 2)()
-    _check(lib().bilu_check_conversions(n_per_thread, seed, out, _stream(stream)))
-    return int(out[0]), int(out[1])
+def check_integer_fp(n_per_thread=1024, seed=1, stream=None):
+    """(roundings, widenings, reciprocals) of the kernels' integer FP64 operations that differ from the
+    hardware's on n_per_thread bit patterns per thread; bilu_check_integer_fp."""
+    out = (C.c_ulonglong * 3)()
+    _check(lib().bilu_check_integer_fp(n_per_thread, seed, out, _stream(stream)))
+    return int(out[0]), int(out[1]), int(out[2])
 
 
 # ---------------------------------------------------------------- generators

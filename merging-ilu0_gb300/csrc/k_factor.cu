@@ -13,7 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "bilu_internal.h"
-#include "k_cvt.cuh"
+#include "k_intfp.cuh"
 
 namespace bilu {
 namespace {
@@ -140,8 +140,9 @@ __global__ void __launch_bounds__(512) k_parilu0(const DevPattern P, int nsys, c
     const bool last = (it == sweeps);
     if (last && !track) break;
     if (FAST && !last) {
-      // __drcp_rn is the correctly rounded reciprocal, the same value as 1.0 / u
-      for (int r = threadIdx.x; r < P.n; r += blockDim.x) rinv[r] = __drcp_rn(cur[__ldg(P.diag + r)]);
+      // the correctly rounded reciprocal, the same value as 1.0 / u, by integer arithmetic (ifp::rcp): off
+      // the FP64 unit, which the sweeps' FMAs and products keep busy
+      for (int r = threadIdx.x; r < P.n; r += blockDim.x) rinv[r] = ifp::rcp(cur[__ldg(P.diag + r)]);
       __syncthreads();
     }
     // entries with dependency pairs (most pairs first, so a warp's lanes run
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(512) k_parilu0(const DevPattern P, int nsys, c
 // exactly that order (zeros of T(J,J) give exact no-op updates).  m is
 // accumulated in FP64 in shared memory and rounded to FT on the way out.
 // FAST (BILU_REDUCE_FAST): the aiU entries are multiplied by the correctly
-// rounded reciprocal of the diagonal (__drcp_rn, one per row, the same value
+// rounded reciprocal of the diagonal (ifp::rcp, one per row, the same value
 // as 1.0 / u) instead of divided -- one FP64 reciprocal per row instead of a
 // division per aiU entry.  The unit-diagonal aiL is unchanged.
 template <typename FT, bool FAST>
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
   // ---- aiU
   double* rinv = M + (P.ail_nnz > P.aiu_nnz ? P.ail_nnz : P.aiu_nnz);  // FAST: n reciprocals
   if (FAST) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) rinv[i] = __drcp_rn(LU[__ldg(P.diag + i)]);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) rinv[i] = ifp::rcp(LU[__ldg(P.diag + i)]);
     __syncthreads();
   }
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -327,7 +328,7 @@ __global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, 
   float* LU = reinterpret_cast<float*>(smem);
   float* M = LU + nnz;                                                  // max(ail_nnz, aiu_nnz)
   float* rinv = M + (P.ail_nnz > P.aiu_nnz ? P.ail_nnz : P.aiu_nnz);  // n
-  for (int k = threadIdx.x; k < nnz; k += blockDim.x) LU[k] = cvt::f32(__ldg(LUg + (size_t)sys * nnz + k));
+  for (int k = threadIdx.x; k < nnz; k += blockDim.x) LU[k] = ifp::f32(__ldg(LUg + (size_t)sys * nnz + k));
   __syncthreads();
   // ---- aiL (unit diagonal)
   for (int i = threadIdx.x; i < n; i += blockDim.x) {

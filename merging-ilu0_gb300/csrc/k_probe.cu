@@ -2,7 +2,7 @@
 // the device, the denominator of the FP64 roofline that the benchmark quotes
 // for the solver kernels (FP64 issue, not HBM, bounds them on GB300); and a
 // check of the kernels' integer FP64 <-> FP32 conversions against the
-// hardware's.
+// hardware's and of the integer reciprocal against __drcp_rn.
 //
 // Every thread runs CH independent DFMA chains (the loop unrolled 4 times), so
 // the 64-cycle latency of a dependent DFMA is covered many times over by the
@@ -18,7 +18,7 @@
 
 #include "bilu.h"
 #include "bilu_internal.h"
-#include "k_cvt.cuh"
+#include "k_intfp.cuh"
 
 namespace bilu {
 namespace {
@@ -82,19 +82,22 @@ cudaError_t best_rate(cudaStream_t st, int sms, long long* d_clk, cudaEvent_t* e
   return e;
 }
 
-// The kernels' FP64 <-> FP32 conversions (k_cvt.cuh: integer forms with the
-// hardware's for what they leave) against the hardware conversions, on n bit
-// patterns per thread of three kinds in turn: any 64-bit pattern; doubles
-// whose exponent sweeps [860, 1165] and 2047 (float subnormal results, the
-// zero / normal / overflow boundaries, infinities, NaNs) with random
-// mantissas, every fourth of them with the 29 bits that rounding drops set
-// to exactly half (ties); any 32-bit pattern for the widening.  bad[0] counts
-// roundings, bad[1] widenings that differ in any bit (NaNs compare by being
-// NaN: both sides are NaN or neither).
-__global__ void k_cvt_check(unsigned long long seed, int n, unsigned long long* __restrict__ bad) {
+// The kernels' integer FP64 operations (k_intfp.cuh: integer forms with the
+// hardware's for what they leave) against the hardware, on n bit patterns per
+// thread.  Conversions, three kinds of double in turn: any 64-bit pattern;
+// doubles whose exponent sweeps [860, 1165] and 2047 (float subnormal
+// results, the zero / normal / overflow boundaries, infinities, NaNs) with
+// random mantissas, every fourth of them with the 29 bits that rounding drops
+// set to exactly half (ties); any 32-bit pattern for the widening.
+// Reciprocals (against __drcp_rn): any 64-bit pattern, every other one with
+// its mantissa reduced to its low 20 bits or its high 32 bits set, every
+// eighth a power of two.  bad[0] counts roundings, bad[1] widenings, bad[2]
+// reciprocals that differ in any bit (NaNs compare by being NaN: both sides
+// are NaN or neither).
+__global__ void k_intfp_check(unsigned long long seed, int n, unsigned long long* __restrict__ bad) {
   const unsigned long long tid = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
   unsigned long long s = seed ^ (0x9e3779b97f4a7c15ull * (tid + 1));
-  unsigned long long nd = 0, nw = 0;
+  unsigned long long nd = 0, nw = 0, nr = 0;
   for (int i = 0; i < n; ++i) {
     s ^= s << 13;
     s ^= s >> 7;
@@ -106,40 +109,48 @@ __global__ void k_cvt_check(unsigned long long seed, int n, unsigned long long* 
       if ((s & 0x3000000000000ull) == 0) u = (u & ~0x1fffffffull) | 0x10000000ull;
     }
     const double d = __longlong_as_double((long long)u);
-    const float a = __double2float_rn(d), b = cvt::f32(d);
+    const float a = __double2float_rn(d), b = ifp::f32(d);
     if (__float_as_uint(a) != __float_as_uint(b) && !(a != a && b != b)) ++nd;
     const float y = __uint_as_float((unsigned)(s >> 17));
-    const double c = (double)y, w = cvt::f64(y);
+    const double c = (double)y, w = ifp::f64(y);
     if (__double_as_longlong(c) != __double_as_longlong(w) && !(c != c && w != w)) ++nw;
+    unsigned long long v = s * 0x2545f4914f6cdd1dull;
+    if ((i & 3) == 1) v &= 0x80000000000fffffull | (0x7ffull << 52);
+    if ((i & 3) == 3) v |= 0x000ffffffff00000ull;
+    if ((i & 7) == 2) v &= 0xfff0000000000000ull;
+    const double dv = __longlong_as_double((long long)v);
+    const double ra = __drcp_rn(dv), rr = ifp::rcp(dv);
+    if (__double_as_longlong(ra) != __double_as_longlong(rr) && !(ra != ra && rr != rr)) ++nr;
   }
   if (nd) atomicAdd(bad, nd);
   if (nw) atomicAdd(bad + 1, nw);
+  if (nr) atomicAdd(bad + 2, nr);
 }
 
 }  // namespace
 }  // namespace bilu
 
-extern "C" bilu_status bilu_check_conversions(int n_per_thread, uint64_t seed, unsigned long long* h_mismatch,
-                                              void* stream) {
+extern "C" bilu_status bilu_check_integer_fp(int n_per_thread, uint64_t seed, unsigned long long* h_mismatch,
+                                             void* stream) {
   using namespace bilu;
-  if (!h_mismatch || n_per_thread < 0) return set_error(BILU_ERR_INVALID, "bilu_check_conversions: bad arguments");
+  if (!h_mismatch || n_per_thread < 0) return set_error(BILU_ERR_INVALID, "bilu_check_integer_fp: bad arguments");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int dev = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return set_error(BILU_ERR_CUDA, std::string("bilu_check_conversions: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) return set_error(BILU_ERR_CUDA, std::string("bilu_check_integer_fp: ") + cudaGetErrorString(e));
   unsigned long long* d_bad = nullptr;
-  if (cudaMalloc(&d_bad, 2 * sizeof(unsigned long long)) != cudaSuccess)
-    return set_error(BILU_ERR_ALLOC, "bilu_check_conversions: cudaMalloc");
-  e = cudaMemsetAsync(d_bad, 0, 2 * sizeof(unsigned long long), st);
+  if (cudaMalloc(&d_bad, 3 * sizeof(unsigned long long)) != cudaSuccess)
+    return set_error(BILU_ERR_ALLOC, "bilu_check_integer_fp: cudaMalloc");
+  e = cudaMemsetAsync(d_bad, 0, 3 * sizeof(unsigned long long), st);
   if (e == cudaSuccess) {
-    k_cvt_check<<<sms * 4, kThreads, 0, st>>>(seed, n_per_thread, d_bad);
+    k_intfp_check<<<sms * 4, kThreads, 0, st>>>(seed, n_per_thread, d_bad);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h_mismatch, d_bad, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_mismatch, d_bad, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaFree(d_bad);
-  if (e != cudaSuccess) return set_error(BILU_ERR_CUDA, std::string("bilu_check_conversions: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) return set_error(BILU_ERR_CUDA, std::string("bilu_check_integer_fp: ") + cudaGetErrorString(e));
   return BILU_OK;
 }
 

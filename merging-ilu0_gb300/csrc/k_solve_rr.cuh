@@ -64,7 +64,7 @@
 #include <cuda_runtime.h>
 
 #include "bilu_internal.h"
-#include "k_cvt.cuh"
+#include "k_intfp.cuh"
 
 namespace bilu {
 namespace {
@@ -154,7 +154,7 @@ __device__ __forceinline__ bool ref_chain_sum(double (&v)[K], Term term, double*
 
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
-// FP64 -> FT and FT -> FP64 with the integer conversions for float (k_cvt.cuh).
+// FP64 -> FT and FT -> FP64 with the integer conversions for float (k_intfp.cuh).
 // Used where the conversions share the SMs with FP64 work (the ISAI paths:
 // preconditioner input and output around the FP32 SpMVs).  The level-scheduled
 // triangular solves keep the hardware conversions: those phases issue no FP64
@@ -163,14 +163,14 @@ __device__ __forceinline__ double fma_t(double a, double b, double c) { return f
 template <typename FT>
 __device__ __forceinline__ FT round_t(double x) {
   if constexpr (sizeof(FT) == 4)
-    return cvt::f32(x);
+    return ifp::f32(x);
   else
     return x;
 }
 template <typename FT>
 __device__ __forceinline__ double widen_t(FT y) {
   if constexpr (sizeof(FT) == 4)
-    return cvt::f64(y);
+    return ifp::f64(y);
   else
     return y;
 }

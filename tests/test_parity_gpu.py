@@ -295,9 +295,10 @@ def test_fp64_rate_probe(cuda):
 
 
 
-def test_integer_conversions_match_hardware(cuda):
-    """The FP32 preconditioner paths round and widen with integer operations (k_cvt.cuh) and leave float
-    subnormal results, infinities and NaNs to the hardware: every bit equal to the hardware conversions on
-    about 160 million patterns of each kind (random doubles, every float exponent boundary with rounding
-    ties, random floats)."""
-    assert bilu.check_conversions(1024, seed=7) == (0, 0)
+def test_integer_fp_matches_hardware(cuda):
+    """The FP32 preconditioner paths round and widen with integer operations, and the FAST ParILU / ISAI take
+    the correctly rounded reciprocal of the diagonal by integer Newton-Raphson (k_intfp.cuh), leaving the
+    special cases to the hardware: every bit equal to the hardware conversions and to __drcp_rn on about 160
+    million patterns of each kind (random doubles, every float exponent boundary with rounding ties, random
+    floats, doubles with short, long and zero mantissas)."""
+    assert bilu.check_integer_fp(1024, seed=7) == (0, 0, 0)
