@@ -126,11 +126,14 @@ struct DevPattern {
   // entries without dependency pairs): the ones the learned warm start predicts
   int n_mlp = 0;
   const int* mlp_ent = nullptr;
-  // ParILU sweep order: entries with dependency pairs (most pairs first), then
-  // lower entries without pairs (l = a / u_jj), then upper entries without
-  // pairs (u = a); warps of one class do the same operations
+  // ParILU sweep order: entries with dependency pairs on or above the diagonal,
+  // then those below it (each most pairs first), then lower entries without
+  // pairs (l = a / u_jj), then upper entries without pairs (u = a); warps of
+  // one class do the same operations, so no FP64 instruction of another class
+  // is issued predicated off (which still costs its FP64-unit slot on GB300)
   const int* pl_ent = nullptr;  // nnz
   int pl_ndep = 0, pl_nlow = 0;
+  int pl_ndep_low = 0;  // the last pl_ndep_low of the pl_ndep entries with pairs are below the diagonal
   // the entries with dependency pairs as a warp-blocked program: slot q
   // (= pl_ent position q < pl_ndep) holds the words k, j << 1 | (j < i), the
   // pair count, then x, y per pair (sum order); word w of slot 32b + l at
@@ -382,7 +385,7 @@ struct bilu_plan {
   std::vector<int> ilu_hdr, ilu_prog;                    // ILU(0) program (DevPattern::ilu_*)
   std::vector<int> sa_off, sa_ci, sa_src, su_off, su_ci, su_src;  // SELL-32 layouts (DevPattern::sa_*, su_*)
   std::vector<int> pl_ent;  // ParILU entry classes (see DevPattern::pl_ent)
-  int pl_ndep = 0, pl_nlow = 0;
+  int pl_ndep = 0, pl_nlow = 0, pl_ndep_low = 0;
   std::vector<int> pl_prog_ptr, pl_prog;  // ParILU program (DevPattern::pl_prog)
   bool has_isai = false;
   std::vector<int> ail_rp, ail_ci, aiu_rp, aiu_ci;

@@ -623,6 +623,7 @@ bilu_status upload(bilu_plan& P) {
   }
   d.pl_ndep = P.pl_ndep;
   d.pl_nlow = P.pl_nlow;
+  d.pl_ndep_low = P.pl_ndep_low;
   if (P.has_isai) {
     d.ail_nnz = P.ail_rp[P.n];
     d.l_diag = P.opts.isai_lower_diag ? 1 : 0;
@@ -820,18 +821,23 @@ bilu_status bilu_plan_create(bilu_plan** out, int n, int nnz, const int* h_rp, c
       if (P->ci[k] < i || P->dep_ptr[k + 1] > P->dep_ptr[k]) P->mlp_ent.push_back(k);
     }
   {
-    std::vector<int> with_deps, lower, upper;
+    std::vector<int> dep_up, dep_low, lower, upper;
     for (int i = 0; i < n; ++i)
       for (int k = P->rp[i]; k < P->rp[i + 1]; ++k) {
         if (P->dep_ptr[k + 1] > P->dep_ptr[k])
-          with_deps.push_back(k);
+          (P->ci[k] < i ? dep_low : dep_up).push_back(k);
         else
           (P->ci[k] < i ? lower : upper).push_back(k);
       }
-    std::stable_sort(with_deps.begin(), with_deps.end(), [&](int a, int b) {
+    auto most_pairs_first = [&](int a, int b) {
       return P->dep_ptr[a + 1] - P->dep_ptr[a] > P->dep_ptr[b + 1] - P->dep_ptr[b];
-    });
+    };
+    std::stable_sort(dep_up.begin(), dep_up.end(), most_pairs_first);
+    std::stable_sort(dep_low.begin(), dep_low.end(), most_pairs_first);
+    std::vector<int> with_deps = dep_up;
+    with_deps.insert(with_deps.end(), dep_low.begin(), dep_low.end());
     P->pl_ndep = (int)with_deps.size();
+    P->pl_ndep_low = (int)dep_low.size();
     P->pl_nlow = (int)lower.size();
     P->pl_ent = with_deps;
     P->pl_ent.insert(P->pl_ent.end(), lower.begin(), lower.end());

@@ -12,6 +12,8 @@
 //   true res.   Bicgstab_common.hpp:294-342
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "bilu_internal.h"
 #include "k_intfp.cuh"
 
@@ -107,7 +109,12 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
 // fast = true (BILU_REDUCE_FAST): the entries below the diagonal are
 // multiplied by reciprocals of the current diagonal, formed once per sweep,
 // instead of divided (n divisions per sweep instead of one per lower entry).
-template <bool FAST>
+// TRACK: the ILU residual is formed (res_tol > 0 or res_out); a kernel of its
+// own, because FP64 instructions skipped under a runtime condition are
+// if-converted into predicated instructions that still take their FP64-unit
+// slots on GB300 (measured: about half of the FP64 warp instructions of the
+// non-tracking sweeps, before this split).
+template <bool FAST, bool TRACK>
 __global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys, const double* __restrict__ A,
                                                     const double* __restrict__ init, double* __restrict__ LUout,
                                                     int sweeps, double res_tol, int* __restrict__ sweeps_out,
@@ -125,44 +132,48 @@ __global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys
   const double* __restrict__ Ag = A + (size_t)sys * nnz;
   const double* Ig = init ? init + (size_t)sys * nnz : Ag;
   double anorm2 = 0.0;
-  for (int k = tid; k < nnz; k += bd) {
-    const double a = __ldg(Ag + k);
-    cur[k] = __ldg(Ig + k);
-    anorm2 = fma(a, a, anorm2);
+  if constexpr (TRACK) {
+    for (int k = tid; k < nnz; k += bd) {
+      const double a = __ldg(Ag + k);
+      cur[k] = __ldg(Ig + k);
+      anorm2 = fma(a, a, anorm2);
+    }
+    anorm2 = block_sum(anorm2, red);
+  } else {
+    for (int k = tid; k < nnz; k += bd) cur[k] = __ldg(Ig + k);
   }
-  const bool track = res_tol > 0.0 || res_out != nullptr;
-  if (track) anorm2 = block_sum(anorm2, red);
   const int lend = P.pl_ndep + P.pl_nlow;
+  const int nhi = P.pl_ndep - P.pl_ndep_low;  // entries with pairs on or above the diagonal: [0, nhi)
   // What every sweep reads about this thread's entries is the same in every
   // sweep, so the first CD entries with dependency pairs (program offset, k,
-  // j << 1 | low, pair count, a_k), the first CL lower entries without pairs
-  // (k, j, a_k) and the first CR diagonal positions are loaded once into
-  // registers (the sweeps' loads were dependent chains through L2: the two
-  // iterates leave little L1); entries past them are read every sweep as
-  // before.  Same arithmetic per entry, so the same bits.  The sizes are the
-  // fastest of those that fit 64 registers (two CTAs of 512 threads per SM)
-  // without spilling, on the 3D 7-point 10x10x10 headline setup: 1.142 ->
-  // 1.065 ms per 4096 systems (CD, CL, CR = 1, 4, 2; 2, 2, 2: 1.125 ms;
-  // 0, 6, 0: 1.081 ms).
+  // j, pair count, a_k), the first CL lower entries without pairs (k, j, a_k)
+  // and the first CR diagonal positions are loaded once into registers (the
+  // sweeps' loads were dependent chains through L2: the two iterates leave
+  // little L1); entries past them are read every sweep as before.  Same
+  // arithmetic per entry, so the same bits.  The sizes are the fastest of
+  // those that fit 64 registers (two CTAs of 512 threads per SM) without
+  // spilling, on the 3D 7-point 10x10x10 headline setup: 1.142 -> 1.065 ms
+  // per 4096 systems (CD, CL, CR = 1, 4, 2; 2, 2, 2: 1.125 ms; 0, 6, 0:
+  // 1.081 ms).
   constexpr int CD = 1, CL = 4, CR = 2;
-  int dk[CD > 0 ? CD : 1], djl[CD > 0 ? CD : 1], dcnt[CD > 0 ? CD : 1], doff[CD > 0 ? CD : 1];
-  double da[CD > 0 ? CD : 1];
+  int dk[CD], dj[CD], dcnt[CD], doff[CD];
+  double da[CD];
 #pragma unroll
   for (int c = 0; c < CD; ++c) {
     const int q = tid + c * bd;
-    dk[c] = djl[c] = dcnt[c] = doff[c] = 0;
+    dk[c] = dj[c] = dcnt[c] = doff[c] = 0;
     da[c] = 0.0;
     if (q < P.pl_ndep) {
       const int o = __ldg(P.pl_prog_ptr + (q >> 5)) + (q & 31);
       dk[c] = __ldg(P.pl_prog + o);
-      djl[c] = __ldg(P.pl_prog + o + 32);
+      dj[c] = __ldg(P.pl_prog + o + 32) >> 1;
       dcnt[c] = __ldg(P.pl_prog + o + 64);
       doff[c] = o + 96;
       da[c] = __ldg(Ag + dk[c]);
     }
   }
-  int lk[CL > 0 ? CL : 1], lj[CL > 0 ? CL : 1];
-  double la[CL > 0 ? CL : 1];
+  int lk[CL], lj[CL];
+  double la[CL];
 #pragma unroll
   for (int c = 0; c < CL; ++c) {
     const int q = P.pl_ndep + tid + c * bd;
@@ -174,7 +185,7 @@ __global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys
       la[c] = __ldg(Ag + lk[c]);
     }
   }
-  int rd[CR > 0 ? CR : 1];
+  int rd[CR];
 #pragma unroll
   for (int c = 0; c < CR; ++c) rd[c] = tid + c * bd < P.n ? __ldg(P.diag + tid + c * bd) : 0;
   __syncthreads();
@@ -183,7 +194,7 @@ __global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys
   for (int it = 0; it <= sweeps; ++it) {
     double r2 = 0.0;
     const bool last = (it == sweeps);
-    if (last && !track) break;
+    if (!TRACK && last) break;
     if (FAST && !last) {
       // the correctly rounded reciprocal, the same value as 1.0 / u, by integer arithmetic (ifp::rcp): off
       // the FP64 unit, which the sweeps' FMAs and products keep busy
@@ -195,8 +206,10 @@ __global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys
     }
     // entries with dependency pairs (most pairs first, so a warp's lanes run
     // alike), read from the warp-blocked program: the words of a slot do not
-    // depend on one another, so their loads overlap
-    auto dep_entry = [&](int k, int jl, int cnt, int off, double a) {
+    // depend on one another, so their loads overlap.  LOW (j < i) is a
+    // compile-time class: the two classes are separate ranges of entries.
+    auto dep_entry = [&](auto low_tag, int k, int j, int cnt, int off, double a) {
+      constexpr bool LOW = decltype(low_tag)::value;
       const int* w = P.pl_prog + off;
       double s = 0.0;
 #pragma unroll 4
@@ -204,54 +217,69 @@ __global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys
         s = fma(cur[__ldg(w)], cur[__ldg(w + 32)], s);
         w += 64;
       }
-      const int j = jl >> 1;
-      const bool low = (jl & 1) != 0;  // j < i
       const double as = a - s;
-      if (track) {  // (A - LU)_ij = (a - s) - l_ij u_jj below the diagonal, (a - s) - u_ij on or above it
-        const double r = low ? fma(-cur[k], cur[__ldg(P.diag + j)], as) : as - cur[k];
+      if constexpr (TRACK) {  // (A - LU)_ij = (a - s) - l_ij u_jj below the diagonal, (a - s) - u_ij on or above it
+        const double r = LOW ? fma(-cur[k], cur[__ldg(P.diag + j)], as) : as - cur[k];
         r2 = fma(r, r, r2);
+        if (last) return;
       }
-      if (!last) nxt[k] = low ? (FAST ? as * rinv[j] : as / cur[__ldg(P.diag + j)]) : as;
+      if constexpr (LOW)
+        nxt[k] = FAST ? as * rinv[j] : as / cur[__ldg(P.diag + j)];
+      else
+        nxt[k] = as;
     };
+    using HiTag = std::integral_constant<bool, false>;
+    using LoTag = std::integral_constant<bool, true>;
 #pragma unroll
-    for (int c = 0; c < CD; ++c)
-      if (tid + c * bd < P.pl_ndep) dep_entry(dk[c], djl[c], dcnt[c], doff[c], da[c]);
-    for (int q = tid + CD * bd; q < P.pl_ndep; q += bd) {
+    for (int c = 0; c < CD; ++c) {
+      const int q = tid + c * bd;
+      if (q < nhi)
+        dep_entry(HiTag{}, dk[c], dj[c], dcnt[c], doff[c], da[c]);
+      else if (q < P.pl_ndep)
+        dep_entry(LoTag{}, dk[c], dj[c], dcnt[c], doff[c], da[c]);
+    }
+    auto dep_loaded = [&](auto tag, int q) {
       const int o = __ldg(P.pl_prog_ptr + (q >> 5)) + (q & 31);
       const int k = __ldg(P.pl_prog + o);
-      dep_entry(k, __ldg(P.pl_prog + o + 32), __ldg(P.pl_prog + o + 64), o + 96, __ldg(Ag + k));
-    }
+      dep_entry(tag, k, __ldg(P.pl_prog + o + 32) >> 1, __ldg(P.pl_prog + o + 64), o + 96, __ldg(Ag + k));
+    };
+    int q = tid + CD * bd;
+    for (; q < nhi; q += bd) dep_loaded(HiTag{}, q);
+    for (; q < P.pl_ndep; q += bd) dep_loaded(LoTag{}, q);
     // lower entries without pairs: the sum is 0, so l = a / u_jj (a - 0 == a exactly)
     auto low_entry = [&](int k, int j, double a) {
-      if (track) {
+      if constexpr (TRACK) {
         const double r = fma(-cur[k], cur[__ldg(P.diag + j)], a);
         r2 = fma(r, r, r2);
+        if (last) return;
       }
-      if (!last) nxt[k] = FAST ? a * rinv[j] : a / cur[__ldg(P.diag + j)];
+      nxt[k] = FAST ? a * rinv[j] : a / cur[__ldg(P.diag + j)];
     };
 #pragma unroll
     for (int c = 0; c < CL; ++c)
       if (P.pl_ndep + tid + c * bd < lend) low_entry(lk[c], lj[c], la[c]);
-    for (int q = P.pl_ndep + tid + CL * bd; q < lend; q += bd) {
-      const int k = __ldg(P.pl_ent + q);
+    for (int q2 = P.pl_ndep + tid + CL * bd; q2 < lend; q2 += bd) {
+      const int k = __ldg(P.pl_ent + q2);
       low_entry(k, __ldg(P.ci + k), __ldg(Ag + k));
     }
     // upper entries without pairs: u = a, no arithmetic; their residual a - u
     // is exactly 0 once one sweep has run, so only the initial guess is checked.
     // Each of the two buffers receives the copies once (sweeps 0 and 1) and
     // keeps them: later sweeps would write the same values again.
-    const bool check_copies = track && it == 0;
-    if (it < 2 || check_copies) {
-      for (int q = lend + tid; q < nnz; q += bd) {
-        const int k = __ldg(P.pl_ent + q);
-        if (check_copies) {
-          const double r = __ldg(Ag + k) - cur[k];
-          r2 = fma(r, r, r2);
-        }
-        if (!last && it < 2) nxt[k] = __ldg(Ag + k);
+    if (TRACK && it == 0) {
+      for (int q2 = lend + tid; q2 < nnz; q2 += bd) {
+        const int k = __ldg(P.pl_ent + q2);
+        const double r = __ldg(Ag + k) - cur[k];
+        r2 = fma(r, r, r2);
+        if (!last) nxt[k] = __ldg(Ag + k);
+      }
+    } else if (it < 2 && !last) {
+      for (int q2 = lend + tid; q2 < nnz; q2 += bd) {
+        const int k = __ldg(P.pl_ent + q2);
+        nxt[k] = __ldg(Ag + k);
       }
     }
-    if (track) {
+    if constexpr (TRACK) {
       const double tot = block_sum(r2, red);
       res = anorm2 > 0.0 ? sqrt(tot / anorm2) : sqrt(tot);
       if (res_tol > 0.0 && res <= res_tol) break;  // uniform: every thread holds the same sum
@@ -585,7 +613,9 @@ cudaError_t launch_parilu0(const DevPattern& p, int nsys, const double* A, const
                            double* res_out, int fast) {
   if (nsys == 0) return cudaSuccess;
   const int smem = p.nnz * 8 * 2 + (fast ? p.n * 8 : 0);
-  auto k = fast ? k_parilu0<true> : k_parilu0<false>;
+  const bool track = res_tol > 0.0 || res_out != nullptr;
+  auto k = fast ? (track ? k_parilu0<true, true> : k_parilu0<true, false>)
+                : (track ? k_parilu0<false, true> : k_parilu0<false, false>);
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   k<<<nsys, threads, smem, st>>>(p, nsys, A, init, lu, sweeps, res_tol, sweeps_out, res_out);
