@@ -64,6 +64,11 @@ struct DevPattern {
   const int* aiu_ci = nullptr;
   // program per ISAI row: blocks {t, k} followed by k entries {c, pos}; rows
   // in blocks of 32, word j of row 32b+l at prog[prog_ptr[b] + 32j + l]
+  // ISAI thread slot -> row: rows by program length, longest first, so a
+  // warp's 32 slots run programs of about the same length; the programs are
+  // warp-blocked in slot order
+  const int* ail_perm = nullptr;
+  const int* aiu_perm = nullptr;
   const int* ail_prog_ptr = nullptr;  // (n+31)/32 + 1 block offsets (words)
   const int* ail_prog = nullptr;      // words t | count << 5 and c | pos << 5 (build_isai)
   const int* aiu_prog_ptr = nullptr;
@@ -390,6 +395,7 @@ struct bilu_plan {
   bool has_isai = false;
   std::vector<int> ail_rp, ail_ci, aiu_rp, aiu_ci;
   std::vector<int> ail_prog_ptr, ail_prog, aiu_prog_ptr, aiu_prog;  // per-row programs, one word per step
+  std::vector<int> ail_perm, aiu_perm;                              // ISAI slot -> row (DevPattern::ail_perm)
   bool general_isai = false;
   std::vector<int> gen_map_ptr, gen_map, gen_pos;
   int* dbuf = nullptr;

@@ -516,6 +516,7 @@ bilu_status upload(bilu_plan& P) {
   }
   const size_t o_suo = put(P.su_off), o_suc = put(P.su_ci), o_sus = put(P.su_src);
   size_t o_alrp = 0, o_alci = 0, o_aurp = 0, o_auci = 0, o_alpp = 0, o_alp = 0, o_aupp = 0, o_aup = 0;
+  size_t o_alperm = 0, o_auperm = 0;
   size_t o_gmp = 0, o_gm = 0, o_gp = 0;
   if (P.general_isai) {
     o_gmp = put(P.gen_map_ptr);
@@ -529,26 +530,36 @@ bilu_status upload(bilu_plan& P) {
     o_auci = put(P.aiu_ci);
     // device layout of the per-row ISAI programs: rows in blocks of 32 (a warp's rows), word j of
     // row 32b+l at off[b] + 32j + l, so a warp's program loads are contiguous lines
-    auto blocked = [&](const std::vector<int>& ptr, const std::vector<int>& prog, std::vector<int>& off,
-                       std::vector<int>& words) {
+    // rows are taken in slot order perm (longest program first), so slot s = 32b+l runs row perm[s]
+    auto blocked = [&](const std::vector<int>& ptr, const std::vector<int>& prog, std::vector<int>& perm,
+                       std::vector<int>& off, std::vector<int>& words) {
+      perm.resize(P.n);
+      for (int i = 0; i < P.n; ++i) perm[i] = i;
+      std::stable_sort(perm.begin(), perm.end(),
+                       [&](int a, int b) { return ptr[a + 1] - ptr[a] > ptr[b + 1] - ptr[b]; });
       const int nb = (P.n + 31) / 32;
       off.assign(nb + 1, 0);
       for (int bk = 0; bk < nb; ++bk) {
         int len = 0;
-        for (int i = 32 * bk; i < std::min(P.n, 32 * bk + 32); ++i) len = std::max(len, ptr[i + 1] - ptr[i]);
+        for (int sl = 32 * bk; sl < std::min(P.n, 32 * bk + 32); ++sl)
+          len = std::max(len, ptr[perm[sl] + 1] - ptr[perm[sl]]);
         off[bk + 1] = off[bk] + 32 * len;
       }
       words.assign((size_t)off[nb], 0);
-      for (int i = 0; i < P.n; ++i)
-        for (int j = 0; j < ptr[i + 1] - ptr[i]; ++j) words[(size_t)off[i / 32] + 32 * j + i % 32] = prog[ptr[i] + j];
+      for (int sl = 0; sl < P.n; ++sl) {
+        const int i = perm[sl];
+        for (int j = 0; j < ptr[i + 1] - ptr[i]; ++j) words[(size_t)off[sl / 32] + 32 * j + sl % 32] = prog[ptr[i] + j];
+      }
     };
     std::vector<int> off, words;
-    blocked(P.ail_prog_ptr, P.ail_prog, off, words);
+    blocked(P.ail_prog_ptr, P.ail_prog, P.ail_perm, off, words);
     o_alpp = put(off);
     o_alp = put(words);
-    blocked(P.aiu_prog_ptr, P.aiu_prog, off, words);
+    o_alperm = put(P.ail_perm);
+    blocked(P.aiu_prog_ptr, P.aiu_prog, P.aiu_perm, off, words);
     o_aupp = put(off);
     o_aup = put(words);
+    o_auperm = put(P.aiu_perm);
   }
   cudaError_t e = cudaMalloc((void**)&P.dbuf, buf.size() * sizeof(int));
   if (e != cudaSuccess) return set_error(BILU_ERR_ALLOC, std::string("plan upload: ") + cudaGetErrorString(e));
@@ -636,6 +647,8 @@ bilu_status upload(bilu_plan& P) {
     d.ail_prog = b + o_alp;
     d.aiu_prog_ptr = b + o_aupp;
     d.aiu_prog = b + o_aup;
+    d.ail_perm = b + o_alperm;
+    d.aiu_perm = b + o_auperm;
   }
   if (P.general_isai) {
     d.gen_map_ptr = b + o_gmp;

@@ -308,7 +308,11 @@ __global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys
 //   U (upper): m_0 = 1 / u_ii; for t = 1..sz-1:
 //        acc = 0; for c = 0..t-1: acc = fma(-m_c, U(J_c,J_t), acc); m_t = acc / U(J_t,J_t)
 // The per-row program lists the structurally nonzero (c, position) pairs in
-// exactly that order (zeros of T(J,J) give exact no-op updates).  m is
+// exactly that order (zeros of T(J,J) give exact no-op updates).  Thread slot
+// s takes row ail_perm[s] / aiu_perm[s]: rows ordered by program length, so a
+// warp's lanes run programs of about the same length (one thread computes a
+// whole row into its own output range, so which thread does it changes no
+// bit).  m is
 // accumulated in FP64 in shared memory and rounded to FT on the way out.
 // FAST (BILU_REDUCE_FAST): the aiU entries are multiplied by the correctly
 // rounded reciprocal of the diagonal (ifp::rcp, one per row, the same value
@@ -326,11 +330,12 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
   const double* __restrict__ LU = LUg + (size_t)sys * nnz;
   double* M = reinterpret_cast<double*>(smem);  // max(ail_nnz, aiu_nnz)
   // ---- aiL
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int sl = threadIdx.x; sl < n; sl += blockDim.x) {
+    const int i = __ldg(P.ail_perm + sl);
     const int beg = __ldg(P.ail_rp + i), sz = __ldg(P.ail_rp + i + 1) - beg;
     double* m = M + beg;
     m[sz - 1] = P.l_diag ? 1.0 / LU[__ldg(P.diag + i)] : 1.0;
-    int q = __ldg(P.ail_prog_ptr + (i >> 5)) + (i & 31);
+    int q = __ldg(P.ail_prog_ptr + (sl >> 5)) + (sl & 31);
     for (int blk = 0; blk < sz - 1; ++blk) {
       const int h = __ldg(P.ail_prog + q);  // t | count << 5; a row's words are 32 apart
       const int ht = h & 31, hc = h >> 5;
@@ -353,11 +358,12 @@ __global__ void __launch_bounds__(512) k_isai(const DevPattern P, int nsys, cons
     for (int i = threadIdx.x; i < n; i += blockDim.x) rinv[i] = ifp::rcp(LU[__ldg(P.diag + i)]);
     __syncthreads();
   }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int sl = threadIdx.x; sl < n; sl += blockDim.x) {
+    const int i = __ldg(P.aiu_perm + sl);
     const int beg = __ldg(P.aiu_rp + i), sz = __ldg(P.aiu_rp + i + 1) - beg;
     double* m = M + beg;
     m[0] = FAST ? rinv[i] : 1.0 / LU[__ldg(P.diag + i)];
-    int q = __ldg(P.aiu_prog_ptr + (i >> 5)) + (i & 31);
+    int q = __ldg(P.aiu_prog_ptr + (sl >> 5)) + (sl & 31);
     for (int blk = 1; blk < sz; ++blk) {
       const int h = __ldg(P.aiu_prog + q);  // t | count << 5; a row's words are 32 apart
       const int ht = h & 31, hc = h >> 5;
@@ -418,11 +424,12 @@ __global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, 
   for (int k = threadIdx.x; k < nnz; k += blockDim.x) LU[k] = ifp::f32(__ldg(LUg + (size_t)sys * nnz + k));
   __syncthreads();
   // ---- aiL (unit diagonal)
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int sl = threadIdx.x; sl < n; sl += blockDim.x) {
+    const int i = __ldg(P.ail_perm + sl);
     const int beg = __ldg(P.ail_rp + i), sz = __ldg(P.ail_rp + i + 1) - beg;
     float* m = M + beg;
     m[sz - 1] = 1.0f;
-    int q = __ldg(P.ail_prog_ptr + (i >> 5)) + (i & 31);
+    int q = __ldg(P.ail_prog_ptr + (sl >> 5)) + (sl & 31);
     // blocks 0 .. sz-2; each block's header (t | count << 5) is loaded while the block before it runs
     int h = sz > 1 ? __ldg(P.ail_prog + q) : 0;
     for (int blk = 0; blk < sz - 1; ++blk) {
@@ -438,11 +445,12 @@ __global__ void __launch_bounds__(512) k_isai_f32(const DevPattern P, int nsys, 
   // ---- aiU
   for (int i = threadIdx.x; i < n; i += blockDim.x) rinv[i] = __frcp_rn(LU[__ldg(P.diag + i)]);
   __syncthreads();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int sl = threadIdx.x; sl < n; sl += blockDim.x) {
+    const int i = __ldg(P.aiu_perm + sl);
     const int beg = __ldg(P.aiu_rp + i), sz = __ldg(P.aiu_rp + i + 1) - beg;
     float* m = M + beg;
     m[0] = rinv[i];
-    int q = __ldg(P.aiu_prog_ptr + (i >> 5)) + (i & 31);
+    int q = __ldg(P.aiu_prog_ptr + (sl >> 5)) + (sl & 31);
     // blocks 1 .. sz-1, headers loaded one block ahead as for aiL
     int h = sz > 1 ? __ldg(P.aiu_prog + q) : 0;
     for (int blk = 1; blk < sz; ++blk) {
