@@ -102,7 +102,7 @@ SECONDARY = [
 # dram__bytes_write.sum) of a 3072-system launch divided by 3072 -- the traffic grows in proportion to the
 # systems of a launch -- and the FP64 pipe (sm__pipe_fp64_cycles_active, percent of peak sustained active).
 RR_NCU = {"kernel": "k_bicgstab_rr_occ<4, 1, float>", "threads_per_system": 256, "smem_staging": 16,
-          "sm__pipe_fp64_cycles_active_pct": 68.5, "dram_bytes_per_system": 189_580,
+          "sm__pipe_fp64_cycles_active_pct": 62.5, "dram_bytes_per_system": 195_600,
           "source": "profiles/k_bicgstab_rr_occ_parilu5_isai_fp32_3d7_10x10x10.md (3072 systems)"}
 
 # systems of the headline workload that both CPU timings run (the GPU line's cpu_baseline and every step of
