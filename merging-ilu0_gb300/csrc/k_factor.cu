@@ -114,8 +114,8 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
 // if-converted into predicated instructions that still take their FP64-unit
 // slots on GB300 (measured: about half of the FP64 warp instructions of the
 // non-tracking sweeps, before this split).
-template <bool FAST, bool TRACK>
-__global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys, const double* __restrict__ A,
+template <bool FAST, bool TRACK, bool SMALL>
+__global__ void __launch_bounds__(SMALL ? 384 : 512, SMALL ? 4 : 2) k_parilu0(const DevPattern P, int nsys, const double* __restrict__ A,
                                                     const double* __restrict__ init, double* __restrict__ LUout,
                                                     int sweeps, double res_tol, int* __restrict__ sweeps_out,
                                                     double* __restrict__ res_out) {
@@ -155,9 +155,11 @@ __global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys
   // spilling, on the 3D 7-point 10x10x10 headline setup: 1.142 -> 1.065 ms
   // per 4096 systems (CD, CL, CR = 1, 4, 2; 2, 2, 2: 1.125 ms; 0, 6, 0:
   // 1.081 ms).
-  constexpr int CD = 1, CL = 4, CR = 2;
-  int dk[CD], dj[CD], dcnt[CD], doff[CD];
-  double da[CD];
+  // SMALL (CTAs of at most 384 threads, n <= 384): four CTAs per SM at 40
+  // registers, which leaves no room for the caches.
+  constexpr int CD = SMALL ? 0 : 1, CL = SMALL ? 0 : 4, CR = SMALL ? 0 : 2;
+  int dk[CD > 0 ? CD : 1], dj[CD > 0 ? CD : 1], dcnt[CD > 0 ? CD : 1], doff[CD > 0 ? CD : 1];
+  double da[CD > 0 ? CD : 1];
 #pragma unroll
   for (int c = 0; c < CD; ++c) {
     const int q = tid + c * bd;
@@ -172,8 +174,8 @@ __global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys
       da[c] = __ldg(Ag + dk[c]);
     }
   }
-  int lk[CL], lj[CL];
-  double la[CL];
+  int lk[CL > 0 ? CL : 1], lj[CL > 0 ? CL : 1];
+  double la[CL > 0 ? CL : 1];
 #pragma unroll
   for (int c = 0; c < CL; ++c) {
     const int q = P.pl_ndep + tid + c * bd;
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(512, 2) k_parilu0(const DevPattern P, int nsys
       la[c] = __ldg(Ag + lk[c]);
     }
   }
-  int rd[CR];
+  int rd[CR > 0 ? CR : 1];
 #pragma unroll
   for (int c = 0; c < CR; ++c) rd[c] = tid + c * bd < P.n ? __ldg(P.diag + tid + c * bd) : 0;
   __syncthreads();
@@ -622,8 +624,11 @@ cudaError_t launch_parilu0(const DevPattern& p, int nsys, const double* A, const
   if (nsys == 0) return cudaSuccess;
   const int smem = p.nnz * 8 * 2 + (fast ? p.n * 8 : 0);
   const bool track = res_tol > 0.0 || res_out != nullptr;
-  auto k = fast ? (track ? k_parilu0<true, true> : k_parilu0<true, false>)
-                : (track ? k_parilu0<false, true> : k_parilu0<false, false>);
+  const bool small = threads <= 384;
+  auto k = small ? (fast ? (track ? k_parilu0<true, true, true> : k_parilu0<true, false, true>)
+                         : (track ? k_parilu0<false, true, true> : k_parilu0<false, false, true>))
+                 : (fast ? (track ? k_parilu0<true, true, false> : k_parilu0<true, false, false>)
+                         : (track ? k_parilu0<false, true, false> : k_parilu0<false, false, false>));
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   k<<<nsys, threads, smem, st>>>(p, nsys, A, init, lu, sweeps, res_tol, sweeps_out, res_out);

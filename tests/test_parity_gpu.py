@@ -50,6 +50,57 @@ def test_parilu0_bitwise(cuda, family, sweeps):
     _compare(g, o, f"ParILU(0) {family} sweeps {sweeps}")
 
 
+def _random_pattern_batch(nsys, seed=3):
+    """A random pattern of the uneven generator (n in [200, 300]) shared by nsys systems whose off-diagonal
+    values are those of the generated system times 1 + U(-0.05, 0.05): unlike the stencil families, many of
+    its entries below the diagonal have ILU(0) dependency pairs."""
+    sn, sz, rp, ci, v, b = bilu.gen_uneven(4, H.SEED, 200, 300, 5, 12)
+    r, c, vv, bb = H.uneven_split(sn, sz, rp, ci, v, b)[0]
+    r, c = np.ascontiguousarray(r - r[0], np.int32), np.ascontiguousarray(c, np.int32)
+    rng = np.random.default_rng(seed)
+    row = np.repeat(np.arange(len(r) - 1), np.diff(r))
+    scale = np.where(c[None, :] == row[None, :], 1.0, 1.0 + 0.05 * rng.uniform(-1.0, 1.0, (nsys, len(c))))
+    vals = np.ascontiguousarray(vv[None, :] * scale)
+    bs = np.ascontiguousarray(np.repeat(bb[None, :], nsys, 0) * (1.0 + 0.1 * rng.uniform(-1.0, 1.0, (nsys, len(bb)))))
+    low_with_pairs = 0
+    cols = [set(c[r[i]:r[i + 1]].tolist()) for i in range(len(r) - 1)]
+    for i in range(len(r) - 1):
+        for j in c[r[i]:r[i + 1]]:
+            if j < i and any(k < j and j in cols[k] for k in cols[i]):
+                low_with_pairs += 1
+    assert low_with_pairs > 50
+    return r, c, vals, bs
+
+
+@pytest.mark.parametrize("precond", [bilu.PRECOND_PARILU0, bilu.PRECOND_PARILU0_ISAI])
+def test_parilu0_lower_entries_with_pairs_bitwise(cuda, precond):
+    """ParILU sweeps (and ISAI on their factors) on a random pattern whose lower entries have dependency
+    pairs, the kernel's own class of entries that no stencil family has, and whose ISAI rows differ in
+    length (the ISAI kernels' row order): the reference order end to end."""
+    rp, ci, v, b = _random_pattern_batch(NSYS)
+    # ISAI on the factors' own pattern (power 1): |T|^2 rows of this pattern pass the 32-entry limit
+    o = H.oracle_pipeline(rp, ci, v, b, precond, sweeps=5, isai_power=1)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, parilu_sweeps=5, isai_power=1)
+    _compare(g, o, f"ParILU(0) random pattern precond {precond}")
+
+
+@pytest.mark.parametrize("precond,fp32", [(bilu.PRECOND_PARILU0, False), (bilu.PRECOND_PARILU0, True),
+                                          (bilu.PRECOND_PARILU0_ISAI, False), (bilu.PRECOND_PARILU0_ISAI, True)])
+def test_parilu0_fast_lower_entries_with_pairs_bitwise(cuda, precond, fp32):
+    """The FAST pipeline on the same random pattern (FAST ParILU sweeps with the diagonal reciprocal, FAST
+    ISAI in FP64 or FP32, the register-resident FAST solve) bit for bit against the oracle's FAST order.
+    (bilu_parilu0, the drop-in for the reference's factorisation, always runs the reference's division.)"""
+    rp, ci, v, b = _random_pattern_batch(NSYS)
+    tol = dict(tol_mode=bilu.TOL_REL, tol=1e-10)
+    g = H.gpu_solve(cuda, rp, ci, v, b, precond=precond, parilu_sweeps=5, isai_power=1, reduction=bilu.REDUCE_FAST,
+                    factor_precision=bilu.FP32 if fp32 else bilu.FP64, threads_per_system=128, **tol)
+    assert g["info"]["solver_kernel"] == 1 and g["info"]["threads"] == 128
+    o = H.oracle_fast(rp, ci, v, b, precond, 128, fp32, sweeps=5, power=1, **tol)
+    for f in ("iters", "conv", "status", "res", "x", "true_res"):
+        H.assert_bitwise(g[f], o[f], f"FAST random pattern precond {precond} fp32={fp32}: {f}")
+    assert np.all(g["conv"] == 1)
+
+
 @pytest.mark.parametrize("family", ["2d5_16x16", "3d7_5x5x5", "3d7_7x7x7"])
 @pytest.mark.parametrize("precond", [bilu.PRECOND_ILU0_ISAI, bilu.PRECOND_PARILU0_ISAI])
 def test_isai_bitwise(cuda, family, precond):
