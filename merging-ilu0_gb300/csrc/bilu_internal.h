@@ -96,6 +96,9 @@ struct DevPattern {
   const int* tp_lo = nullptr;
   const int2* tp_up_hdr = nullptr;
   const int* tp_up = nullptr;
+  // the most entries of any row of the lower / upper solve program (the
+  // solves run no product slot past it); kTrsvPrefetch when not known
+  int tp_maxcnt_lo = kTrsvPrefetch, tp_maxcnt_up = kTrsvPrefetch;
   // ILU(0) program of the register-resident solver's merged form (n <= 1024),
   // per lower level: header {off, w, len, 0}; slot s word j at prog[off + j*w + s]:
   // word 0 = number of op words that follow; ops per entry k of the row in

@@ -631,6 +631,13 @@ bilu_status upload(bilu_plan& P) {
     d.tp_lo = b + o_tl;
     d.tp_up_hdr = reinterpret_cast<const int2*>(b + o_tuh);
     d.tp_up = b + o_tu;
+    int ml = 0, mu = 0;
+    for (int i = 0; i < P.n; ++i) {
+      ml = std::max(ml, P.diag[i] - P.rp[i]);
+      mu = std::max(mu, P.rp[i + 1] - P.diag[i] - 1);
+    }
+    d.tp_maxcnt_lo = ml;
+    d.tp_maxcnt_up = mu;
   }
   d.pl_ndep = P.pl_ndep;
   d.pl_nlow = P.pl_nlow;

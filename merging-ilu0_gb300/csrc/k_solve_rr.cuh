@@ -242,15 +242,33 @@ __device__ __forceinline__ void rows_acc_sell(const VT* __restrict__ val, const 
 template <bool UPPER, typename FT, bool REF>
 __device__ __forceinline__ void tri_solve(const int2* __restrict__ hdr, const int* __restrict__ prog, int nlev,
                                           const FT* __restrict__ F, const FT* __restrict__ rinv, FT* y, double* zd,
-                                          int tid, int nt) {
+                                          int tid, int nt, int maxcnt) {
   constexpr int PF = kTrsvPrefetch;
+  // maxcnt: the most entries of any row of this triangle (the plan's
+  // DevPattern::tp_maxcnt_*).  With FP64 factors, triangles whose rows have at
+  // most two entries (5-point stencils) run a copy of the row code with two
+  // product slots instead of kTrsvPrefetch: a guarded FMA can be if-converted
+  // into a predicated one, which still takes its FP64-unit slot on GB300.
+  // Measured (CUDA events): 2D 16x16 reference order 1.01 -> 1.12M systems/s,
+  // FAST with the reference's stopping rule 84.2 -> 68.7 ms, 24x24 414k ->
+  // 423k; 3D 10x10x10 (three entries per row) unchanged.  The choice is one
+  // uniform branch between two fully unrolled copies (a per-slot runtime bound
+  // cost the 3D solves 5-8 %); FP32 factors keep the single copy (their FMAs
+  // use the FP32 pipe, and the second copy cost the FP32 3D solve 4 %).
+  const bool two = sizeof(FT) == 8 && maxcnt <= 2;
   auto row = [&](int rec, const int (&e)[PF], int off, int w, int s) {
     const int i = rec & 1023, cnt = rec >> 10;
     if (REF) {
       FT acc = FT(0);
+      if (two) {
 #pragma unroll
-      for (int j = 0; j < PF; ++j)
-        if (j < cnt) acc = fma_t(F[e[j] >> 10], y[e[j] & 1023], acc);
+        for (int j = 0; j < 2; ++j)
+          if (j < cnt) acc = fma_t(F[e[j] >> 10], y[e[j] & 1023], acc);
+      } else {
+#pragma unroll
+        for (int j = 0; j < PF; ++j)
+          if (j < cnt) acc = fma_t(F[e[j] >> 10], y[e[j] & 1023], acc);
+      }
       for (int j = PF; j < cnt; ++j) {
         const int en = __ldg(prog + off + w + j * w + s);
         acc = fma_t(F[en >> 10], y[en & 1023], acc);
@@ -266,9 +284,15 @@ __device__ __forceinline__ void tri_solve(const int2* __restrict__ hdr, const in
       return;
     }
     FT acc = y[i];
+    if (two) {
 #pragma unroll
-    for (int j = 0; j < PF; ++j)
-      if (j < cnt) acc = fma_t(-F[e[j] >> 10], y[e[j] & 1023], acc);
+      for (int j = 0; j < 2; ++j)
+        if (j < cnt) acc = fma_t(-F[e[j] >> 10], y[e[j] & 1023], acc);
+    } else {
+#pragma unroll
+      for (int j = 0; j < PF; ++j)
+        if (j < cnt) acc = fma_t(-F[e[j] >> 10], y[e[j] & 1023], acc);
+    }
     for (int j = PF; j < cnt; ++j) {
       const int en = __ldg(prog + off + w + j * w + s);
       acc = fma_t(-F[en >> 10], y[en & 1023], acc);
@@ -322,8 +346,8 @@ __device__ __forceinline__ void tri_solve(const int2* __restrict__ hdr, const in
 template <typename FT, bool REF>
 __device__ __forceinline__ void lu_apply(const DevPattern& P, const FT* __restrict__ F, const FT* __restrict__ rinv,
                                          FT* y, double* zd, int tid, int nt) {
-  tri_solve<false, FT, REF>(P.tp_lo_hdr, P.tp_lo, P.nlev_lo, F, rinv, y, zd, tid, nt);
-  tri_solve<true, FT, REF>(P.tp_up_hdr, P.tp_up, P.nlev_up, F, rinv, y, zd, tid, nt);
+  tri_solve<false, FT, REF>(P.tp_lo_hdr, P.tp_lo, P.nlev_lo, F, rinv, y, zd, tid, nt, P.tp_maxcnt_lo);
+  tri_solve<true, FT, REF>(P.tp_up_hdr, P.tp_up, P.nlev_up, F, rinv, y, zd, tid, nt, P.tp_maxcnt_up);
 }
 
 // The reference-order SpMV rows (row_ref, the reference's warp-per-row tree
