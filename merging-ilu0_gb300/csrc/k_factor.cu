@@ -114,11 +114,13 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
 // if-converted into predicated instructions that still take their FP64-unit
 // slots on GB300 (measured: about half of the FP64 warp instructions of the
 // non-tracking sweeps, before this split).
+// SMALL: CTAs of at most 384 threads (n <= 384), bounded for four CTAs per SM
+// instead of two (the per-entry register caches below do not fit it).
 template <bool FAST, bool TRACK, bool SMALL>
-__global__ void __launch_bounds__(SMALL ? 384 : 512, SMALL ? 4 : 2) k_parilu0(const DevPattern P, int nsys, const double* __restrict__ A,
-                                                    const double* __restrict__ init, double* __restrict__ LUout,
-                                                    int sweeps, double res_tol, int* __restrict__ sweeps_out,
-                                                    double* __restrict__ res_out) {
+__global__ void __launch_bounds__(SMALL ? 384 : 512, SMALL ? 4 : 2)
+    k_parilu0(const DevPattern P, int nsys, const double* __restrict__ A, const double* __restrict__ init,
+              double* __restrict__ LUout, int sweeps, double res_tol, int* __restrict__ sweeps_out,
+              double* __restrict__ res_out) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double red[32];
   const int sys = blockIdx.x;

@@ -147,7 +147,8 @@ extern "C" bilu_status bilu_check_integer_fp(int n_per_thread, uint64_t seed, un
     k_intfp_check<<<sms * 4, kThreads, 0, st>>>(seed, n_per_thread, d_bad);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h_mismatch, d_bad, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h_mismatch, d_bad, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaFree(d_bad);
   if (e != cudaSuccess) return set_error(BILU_ERR_CUDA, std::string("bilu_check_integer_fp: ") + cudaGetErrorString(e));
